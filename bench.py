@@ -1,0 +1,361 @@
+#!/usr/bin/env python
+"""Benchmark: <Map^3> triplets/s over a Latin-hypercube batch of cosmologies.
+
+Workload (the batched configuration): cosmologies from a seeded Latin
+hypercube (Om in [0.2,0.4], sigma8 in [0.7,0.9], h in [0.6,0.8],
+w in [-1.2,-0.8], ns in [0.92,1.0], Ob=0.048, z_max=3), source
+n(z) ~ z^2 exp(-(z/0.5)^1.5), 10 log-spaced aperture radii 1..32 arcmin ->
+220 triplets per cosmology; every (cosmology, triplet) is one adaptive
+<Map^3> integral at relative tolerance 1e-4 (the reference's MapMapMap
+settings, l in [1, 10/theta_min]). One step = one batch of C cosmologies: the
+GPU table build (set_cosmology) plus all C*220 integrals in the FP32
+integrand. Inputs are synthetic (no data files are read).
+
+--impl reference times the CPU FP64 restatement of the reference (the
+oracle; the reference itself does not build on this machine) on the host
+cores, one integral per step, on the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Map3 triplets/s at <=1e-3 rel err vs FP64: surrogate+FP32 vs plain FP64, 1 GB300"
+ARCMIN = 2.9088820866e-4
+LHS_SEED = 20261203
+N_LHS = 4096
+SFU_PER_NODE = 49  # SFU ops (ex2/lg2/rcp) per line-of-sight node of the FP32 BiHalofit evaluation
+NNODE = 96
+
+
+def lhs_cosmologies(n=N_LHS, seed=LHS_SEED):
+    """Latin hypercube: per dimension a random permutation of n strata plus a
+    uniform jitter inside each stratum (numpy default_rng(seed))."""
+    rng = np.random.default_rng(seed)
+    box = [("om", 0.2, 0.4), ("sigma8", 0.7, 0.9), ("h", 0.6, 0.8), ("w", -1.2, -0.8), ("ns", 0.92, 1.0)]
+    cols = {}
+    for name, lo, hi in box:
+        u = (rng.permutation(n) + rng.uniform(size=n)) / n
+        cols[name] = lo + u * (hi - lo)
+    out = []
+    for i in range(n):
+        om = float(cols["om"][i])
+        out.append(dict(h=float(cols["h"][i]), sigma8=float(cols["sigma8"][i]), omb=0.048, omc=om - 0.048,
+                        ns=float(cols["ns"][i]), w=float(cols["w"][i]), om=om, ow=1 - om, zmax=3.0))
+    return out
+
+
+def thetas_220():
+    radii = np.exp(np.linspace(np.log(1.0), np.log(32.0), 10)) * ARCMIN
+    t = []
+    for i in range(10):
+        for j in range(i, 10):
+            for k in range(j, 10):
+                t.append((radii[i], radii[j], radii[k]))
+    return np.array(t)
+
+
+def nz_config():
+    zs = np.arange(3001) * 1e-3
+    ns = zs ** 2 * np.exp(-(zs / 0.5) ** 1.5)
+    return zs, ns
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle sampling during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.t.join(timeout=2)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_env():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+# ---------------------------------------------------------------------------
+def run_ours(args):
+    import torch
+
+    import threepoint_gb300 as tp
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    ctx = tp.Context(local)
+    stream = torch.cuda.ExternalStream(ctx.stream_handle, device=local)
+    cosmos_all = lhs_cosmologies()
+    zs, ns = nz_config()
+    nz = tp.rebin_n_of_z(zs, ns, 256, 3.0)
+    th = thetas_220()
+    C = args.cosmo_per_step
+    nt = len(th)
+    nj = C * nt
+    dev = torch.device("cuda", local)
+    job_cosmo = torch.arange(C, dtype=torch.int32, device=dev).repeat_interleave(nt)
+    job_theta = torch.tensor(np.tile(th, (C, 1)), dtype=torch.float64, device=dev)
+    out = torch.zeros(nj, dtype=torch.float64, device=dev)
+    err = torch.zeros_like(out)
+    nev = torch.zeros(nj, dtype=torch.int64, device=dev)
+    nlive = torch.zeros(nj, dtype=torch.int64, device=dev)
+    status = torch.zeros(nj, dtype=torch.int32, device=dev)
+    lmax = 0.0 if args.lmax == "ref" else float(args.lmax)
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=dev)  # > 129 MB L2
+
+    def cosmo_batch(step):
+        off = ((rank * (args.steps + args.warmup) + step) * C) % (N_LHS - C)
+        return [tp.cosmology(**c) for c in cosmos_all[off:off + C]]
+
+    def one_step(step, timing):
+        batch = cosmo_batch(step)
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+        with torch.cuda.stream(stream):
+            ev[0].record(stream)
+            ctx.set_cosmologies(batch, nz)
+            ev[1].record(stream)
+            ctx.map3_jobs_device(job_cosmo, job_theta, out, err, nev, status, lMax=lmax, rel_tol=1e-4,
+                                 precision=tp.FP32, nlive=nlive)
+            ev[2].record(stream)
+        if timing is not None:
+            timing.append(ev)
+
+    # warm-up
+    for s in range(args.warmup):
+        one_step(s, None)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    sampler = ClockSampler(local)
+    sampler.start()
+    timings = []
+    live_total = 0
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for s in range(args.steps):
+        flush.zero_()  # L2 flush between steps (outside the per-step events)
+        torch.cuda.synchronize()
+        one_step(args.warmup + s, timings)
+        torch.cuda.synchronize()
+        live_total += int(nlive.sum().item())
+        bad = int((status != 0).sum().item())
+        if bad:
+            print(f"warning: {bad} integrals hit a cap in step {s}", file=sys.stderr)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    clocks = sampler.stop()
+    step_ms = [t[0].elapsed_time(t[2]) for t in timings]
+    map3_ms = [t[1].elapsed_time(t[2]) for t in timings]
+    tot_ms = sum(step_ms)
+    if dist:
+        tt = torch.tensor([tot_ms], device=dev)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        tot_ms = float(tt.item())
+    integrals = nj * args.steps * world
+    value = integrals / (tot_ms * 1e-3)
+
+    # accuracy vs plain FP64 on a subset of the last batch (outside the timed region)
+    sub = list(range(0, nt, max(1, nt // 12)))
+    batch = cosmo_batch(args.warmup + args.steps - 1)[:1]
+    ctx.set_cosmologies(batch, nz)
+    v32 = ctx.map3_batch(th[sub], precision=tp.FP32)
+    v64 = ctx.map3_batch(th[sub], precision=tp.FP64)
+    nz_mask = v64 != 0  # strongly unequal triplets integrate to exactly 0 (first rule all-zero), as in the reference
+    max_rel = float(np.max(np.abs(v32[nz_mask] - v64[nz_mask]) / np.abs(v64[nz_mask])))
+    zeros_agree = bool(np.array_equal(v32 == 0, v64 == 0))
+
+    # e2e: the public host API (host inputs, host outputs) for the same steps
+    e2e_steps = max(1, min(args.steps, 3))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for s in range(e2e_steps):
+        ctx.set_cosmologies(cosmo_batch(args.warmup + s), nz)
+        res = ctx.map3_batch(th, precision=tp.FP32, check=False)
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - t0
+    e2e_val = nj * e2e_steps / e2e_s
+    h2d = C * 72 + 256 * 8 + nj * (3 * 8 + 4)
+    d2h = nj * (8 + 8 + 8 + 4)
+
+    # roofline of the dominant kernel (k_map3<float>): SFU ops of the live points
+    sfu_peak, f32_peak, f64_peak = tp.pipe_peaks(local)
+    live_per_launch = live_total / args.steps
+    map3_avg_s = statistics.mean(map3_ms) * 1e-3
+    achieved = live_per_launch * NNODE * SFU_PER_NODE / map3_avg_s
+
+    if dist:
+        dist.barrier()
+    if rank != 0:
+        return None
+    res = {
+        "metric": METRIC,
+        "value": value,
+        "unit": "triplets/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": tot_ms / args.steps,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic",
+        "config": {"workload": f"{C} LHS cosmologies x 220 theta-triplets per step (4096-cosmology LHS batch)",
+                   "cosmologies_per_step": C, "triplets": nt, "rel_tol": 1e-4,
+                   "l_range": "[1, 10/theta_min]" if lmax == 0 else f"[1, {lmax:g}]",
+                   "l2": "flushed between steps (256 MB write)", "parallelism": f"replicas x{world}",
+                   "max_rel_err_fp32_vs_fp64": max_rel, "fp64_check_integrals": int(v64.size),
+                   "zero_valued_agree": zeros_agree},
+        "e2e": {"value": e2e_val, "unit": "triplets/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "gpu_launches": 7 * args.steps,
+        "roofline": {"bound": "sfu", "achieved": achieved / 1e9, "peak": sfu_peak / 1e9, "unit": "Gop/s",
+                     "frac": achieved / sfu_peak, "traffic": None,
+                     "peak_source": "measured now by tp_pipe_peaks (ex2.approx.f32 loop, whole device)",
+                     "kernel": "k_map3<float>", "kernel_ms_per_launch": map3_avg_s * 1e3,
+                     "fp32_fma_peak_tflops": f32_peak / 1e12, "fp64_fma_peak_tflops": f64_peak / 1e12},
+        "clocks": clocks,
+        "wall_s": wall,
+    }
+    if not args.no_cpu_baseline:
+        res["cpu_baseline"] = cpu_baseline(args, sample_triplets=args.cpu_sample)
+    return res
+
+
+def cpu_baseline(args, sample_triplets=2):
+    """The CPU FP64 restatement on the host cores, a bounded sample of the
+    same workload: the first LHS cosmology, sample_triplets triplets."""
+    import oracle
+
+    n = os.cpu_count() or 1
+    oracle.set_threads(n)
+    c = lhs_cosmologies()[0]
+    zs, ns = nz_config()
+    nz = oracle.read_n_of_z(zs, ns, 256, 3.0)
+    th = thetas_220()
+    pick = [th[i] for i in np.linspace(0, len(th) - 1, sample_triplets).astype(int)]
+    t0 = time.perf_counter()
+    T = oracle.Tables(c, nz)
+    for t in pick:
+        T.map3(list(t))
+    dt = time.perf_counter() - t0
+    return {"value": len(pick) / dt, "unit": "triplets/s", "cores": n, "kind": "port",
+            "sample": f"{len(pick)} triplets of LHS cosmology 0 incl. its table build, FP64, {n} threads"}
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return None
+    import oracle
+
+    n = os.cpu_count() or 1
+    oracle.set_threads(n)
+    cos = lhs_cosmologies()
+    zs, ns = nz_config()
+    nz = oracle.read_n_of_z(zs, ns, 256, 3.0)
+    th = thetas_220()
+    T = oracle.Tables(cos[0], nz)
+    # one integral per step, stepping through the 220 triplets with a stride
+    order = [int(i) for i in np.linspace(0, len(th) - 1, args.steps + args.warmup)]
+    for s in range(args.warmup):
+        T.map3(list(th[order[s]]))
+    times = []
+    for s in range(args.steps):
+        t0 = time.perf_counter()
+        T.map3(list(th[order[args.warmup + s]]))
+        times.append(time.perf_counter() - t0)
+    tot = sum(times)
+    value = args.steps / tot
+    return {
+        "metric": METRIC, "value": value, "unit": "triplets/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": tot / args.steps * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
+        "config": {"workload": "1 (cosmology, theta-triplet) integral per step of the 4096-LHS x 220 batch",
+                   "rel_tol": 1e-4, "l_range": "[1, 10/theta_min]"},
+        "cpu_baseline": {"value": value, "unit": "triplets/s", "cores": n, "kind": "port",
+                         "sample": f"{args.steps} integrals of LHS cosmology 0 (FP64 CPU restatement, {n} threads)"},
+        "e2e": {"value": value, "unit": "triplets/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--cosmo-per-step", type=int, default=16)
+    ap.add_argument("--lmax", default="ref")
+    ap.add_argument("--cpu-sample", type=int, default=2)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
+    res = run_reference(args) if args.impl == "reference" else run_ours(args)
+    if res is not None:
+        print(json.dumps(res))
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,174 @@
+/*
+ * threepoint_gb300 -- C ABI of the GB300 (sm_103a) implementation of the
+ * threepoint model-evaluation path: the line-of-sight projected BiHalofit
+ * convergence bispectrum b_kappa, <Map^3>, the shear-3PCF natural components
+ * Gamma_i and the <Map^3> covariance terms T1, T2, T4.
+ *
+ * Conventions: plain pointers and sizes; host buffers unless a name ends in
+ * _device; angles in radians; FP64 results. Every call returns an int status
+ * (TP_OK == 0) and never exits the process; tp_status_string() and
+ * tp_last_error() describe failures. One context = one CUDA device + one
+ * stream; calls on one context are not thread-safe.
+ *
+ * Each entry point names the reference interface it replaces (file:line in
+ * the reference project sheydenreich/threepoint).
+ */
+#ifndef THREEPOINT_GB300_H
+#define THREEPOINT_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+enum {
+  TP_OK = 0,
+  TP_ERR_ARG = 1,         /* invalid argument */
+  TP_ERR_IO = 2,          /* file missing or unreadable */
+  TP_ERR_FORMAT = 3,      /* file content not in the expected format */
+  TP_ERR_CUDA = 4,        /* CUDA runtime error */
+  TP_ERR_STATE = 5,       /* call out of order (e.g. no cosmology set) */
+  TP_ERR_CAPACITY = 6,    /* an adaptive integral hit its region/sweep cap */
+  TP_ERR_NOMEM = 7
+};
+
+/* precision of the integrand evaluation */
+enum {
+  TP_FP64 = 0,  /* plain FP64 BiHalofit: the correctness path */
+  TP_FP32 = 1   /* FP32 BiHalofit with compensated (Kahan) line-of-sight sums */
+};
+
+/* error norm of a vector integrand (cubature.h) */
+enum { TP_NORM_INDIVIDUAL = 0, TP_NORM_PAIRED, TP_NORM_L2, TP_NORM_L1, TP_NORM_LINF };
+
+/* survey geometry of the covariance (calculateApertureStatisticsCovariance.cu:111-130) */
+enum { TP_GEOM_CIRCLE = 0, TP_GEOM_SQUARE = 1, TP_GEOM_INFINITE = 2 };
+
+/* Cosmological parameters; same fields and meaning as the reference's class
+ * cosmology (cuda_version/cosmology.cuh:13-29). */
+typedef struct {
+  double h, sigma8, omb, omc, ns, w, om, ow, zmax;
+} tp_cosmology;
+
+typedef struct tp_ctx tp_ctx;
+
+const char* tp_status_string(int status);
+const char* tp_last_error(const tp_ctx* ctx);
+/* library version string */
+const char* tp_version(void);
+
+/* ---- inputs (host only, no GPU needed) --------------------------------- */
+
+/* Replaces cosmology::cosmology(const std::string&) (cuda_version/cosmology.cu:11-78):
+ * reads h, sigma_8, Omega_b, n_s, w, Omega_m, z_max; sets ow = 1-om, omc = om-omb. */
+int tp_cosmology_from_file(const char* path, tp_cosmology* out);
+
+/* Replaces read_n_of_z (cuda_version/helpers.cu:9-128): rebins an ASCII
+ * "z n(z)" table to n_bins bins at i*zmax/n_bins and normalises sum(n)*dz=1. */
+int tp_read_n_of_z(const char* path, int n_bins, double zmax, double* nz_out);
+
+/* The rebinning/normalisation step of read_n_of_z applied to an in-memory
+ * table of nf (z, n) pairs with uniform z spacing. */
+int tp_rebin_n_of_z(const double* z, const double* n, int nf, int n_bins, double zmax, double* nz_out);
+
+/* Replaces read_thetas (cuda_version/helpers.cu:176-200): one value per line.
+ * Writes at most cap values, *n_out = number read. */
+int tp_read_thetas(const char* path, double* out, int cap, int* n_out);
+
+/* convert_angle_to_rad (cuda_version/helpers.cu:130-153); unit "arcmin", "deg" or "rad" */
+int tp_convert_angle_to_rad(double value, const char* unit, double* out);
+
+/* ---- context ------------------------------------------------------------ */
+int tp_ctx_create(int device, tp_ctx** out);
+int tp_ctx_destroy(tp_ctx* ctx);
+/* the context's CUDA stream (a cudaStream_t), for callers that order their own
+ * work or CUDA events with the library's asynchronous entry points */
+void* tp_ctx_stream(tp_ctx* ctx);
+
+/* Measured throughput of the pipes that bound the integrand kernels, whole
+ * device: out[0] ex2.approx.f32 (SFU) ops/s, out[1] FP32 FMA/s, out[2] FP64 FMA/s. */
+int tp_pipe_peaks(int device, double* out);
+
+/* Replaces copyConstants() + set_cosmology(cosmo, nz, Pk, dk, kmin, kmax)
+ * (cuda_version/bispectrum.cu:90-219), batched: builds on the GPU, in FP64,
+ * the z-tables (f_K, g, D1, r_sigma, n_eff, ncur) of n_cosmo cosmologies and
+ * the per-node line-of-sight coefficients derived from them.
+ *   nz: 256 values per cosmology (nz_stride = 256) or one shared row
+ *       (nz_stride = 0), as produced by tp_read_n_of_z.
+ *   pk: optional (NULL -> Eisenstein & Hu): 256 log-spaced linear P(k) values
+ *       per cosmology with dk, kmin, kmax as from convert_Pk (helpers.cu:202-214). */
+int tp_set_cosmologies(tp_ctx* ctx, const tp_cosmology* cosmo, int n_cosmo, const double* nz, int nz_stride,
+                       const double* pk, double dk, double kmin, double kmax);
+
+/* Shape noise and galaxy density used by the power spectrum P(ell) of the
+ * covariance (globals sigma, n, constant_powerspectrum of the reference:
+ * bispectrum.cu:21-23, initCovariance apertureStatisticsCovariance.cu:30-45). */
+int tp_set_shape_noise(tp_ctx* ctx, double sigma_eps, double n_gal_per_rad2, int constant_powerspectrum);
+
+/* Copies cosmology i's FP64 tables to the host: 6*256 doubles
+ * (f_K, g, D1, r_sigma, n_eff, ncur) followed by norm. */
+int tp_get_tables(tp_ctx* ctx, int cosmo_index, double* out);
+
+/* ---- point evaluations (no cubature) ------------------------------------ */
+
+/* bkappa(ell1, ell2, ell3) (cuda_version/bispectrum.cu:293-309) for n points:
+ * ell is [n][3], cosmo_index[n] selects the cosmology (NULL -> cosmology 0). */
+int tp_bkappa_batch(tp_ctx* ctx, const int* cosmo_index, const double* ell, long n, int precision, double* out);
+
+/* Pell(ell) (cuda_version/bispectrum.cu:511-529, device branch) for n values. */
+int tp_pell_batch(tp_ctx* ctx, int cosmo_index, const double* ell, long n, int precision, double* out);
+
+/* ---- adaptive integrals ------------------------------------------------- */
+
+/* Replaces MapMapMap(thetas, phiMin, phiMax, lMin) (cuda_version/apertureStatistics.cu:201-230;
+ * declared apertureStatistics.cuh:106) for every (cosmology, triplet) pair:
+ * out[c * n_trip + t] = <Map^3>(thetas[3t..3t+2]) of cosmology c, by
+ * h-adaptive Genz-Malik cubature over (l1, l2, phi) on [lMin, lMax]^2 x
+ * [phiMin, phiMax] with relative tolerance rel_tol (reference: 1e-4),
+ * divided by (2 pi)^3. lMax <= 0 selects the reference bound 10/theta_min.
+ * err (optional) receives the error estimate, neval (optional) the number of
+ * integrand points. Returns TP_ERR_CAPACITY if any integral hit a cap (its
+ * value is still written; status_out[i] != 0 flags which, if given). */
+int tp_map3_batch(tp_ctx* ctx, const int* cosmo_index, int n_cosmo, const double* thetas, int n_trip,
+                  double phi_min, double phi_max, double l_min, double l_max, double rel_tol, int precision,
+                  double* out, double* err, int64_t* neval, int* status_out);
+
+/* Same as tp_map3_batch with device-resident inputs/outputs, asynchronous on
+ * the context stream (no host synchronisation). job_cosmo/job_theta are
+ * [n_jobs] and [n_jobs][3] device arrays; out/err are [n_jobs]; neval, nlive
+ * and status are [n_jobs] (each may be NULL). nlive counts the cubature points
+ * whose filter product is non-zero, i.e. whose line-of-sight sum was evaluated. */
+int tp_map3_jobs_device(tp_ctx* ctx, const int* job_cosmo_device, const double* job_theta_device, int n_jobs,
+                        double phi_min, double phi_max, double l_min, double l_max, double rel_tol, int precision,
+                        double* out_device, double* err_device, int64_t* neval_device, int64_t* nlive_device,
+                        int* status_device);
+
+/* Replaces gamma0..gamma3(x1, x2, x3, z_max) (cuda_version/gamma.cu:98-148;
+ * gamma.cuh:56-97): natural components of the shear 3PCF for n triangles
+ * x[3i..3i+2] (radians) of one cosmology, by Ogata Hankel quadrature
+ * (h = 0.1, 32 nodes) inside a 3-D adaptive cubature over (z, phi, psi) with
+ * relative tolerance rel_tol (reference: 1e-3). comp_mask bit k selects
+ * Gamma^k; out is [n][4] complex as 8 doubles (re, im per component); the
+ * orthocentre-to-centroid rotation is applied (gamma.cuh:25). */
+int tp_gamma_batch(tp_ctx* ctx, int cosmo_index, const double* x, int n, int comp_mask, double rel_tol,
+                   int precision, double* out, int* status_out);
+
+/* Ogata nodes/weights of compute_weights_bessel (cuda_version/gamma.cu:13-56):
+ * out[4][33] = psi(J6), product(J6), psi(J2), product(J2). */
+int tp_ogata_weights(double* out);
+
+/* Covariance terms of <Map^3> (cuda_version/apertureStatisticsCovariance.cu):
+ * T1_total, T2_total, T4_total (:272-683) for pairs of triplets.
+ * term: 1, 2 or 4; geometry TP_GEOM_*; theta_max [rad] and area [rad^2] as in
+ * covarianceParameters (cosmology.cu:92-170). out[i] = T_term(th123[i], th456[i]). */
+int tp_cov_total_batch(tp_ctx* ctx, int cosmo_index, int term, int geometry, double theta_max, double area,
+                       const double* th123, const double* th456, int n, int precision, double* out,
+                       int* status_out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* THREEPOINT_GB300_H */

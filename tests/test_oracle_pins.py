@@ -1,0 +1,128 @@
+"""The oracle against the reference's own host code (golden vectors generated by
+tests/golden/make_golden.py from the reference's bispectrum.cu / hcubature.cpp)."""
+import ctypes as C
+import json
+import math
+import os
+
+import numpy as np
+import pytest
+
+import oracle as O
+from conftest import COSMO1
+
+GOLD = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "reference_host.json")))
+
+
+def test_nz_restatement_matches_fixture(nz256):
+    assert np.array_equal(np.array(GOLD["nz256"]), nz256)
+
+
+def test_tables_match_reference(oracle_tables):
+    a = oracle_tables.arrays()
+    for n in ("f_K", "g", "D1", "r_sigma", "n_eff", "ncur"):
+        ref = np.array(GOLD["tables"][n])
+        rel = np.abs(a[n] - ref) / np.maximum(np.abs(ref), 1e-300)
+        # f_K/g differ from the reference only through the 15-digit Gauss table
+        assert rel.max() < 1e-12, (n, rel.max())
+    assert a["norm"] == GOLD["norm"]
+
+
+def test_scalar_functions_match_reference(oracle_tables):
+    T = oracle_tables
+    for k, v in GOLD["linear_pk"]:
+        assert T.linear_pk(k) == pytest.approx(v, rel=1e-14)
+    for r, j, v in GOLD["sigmam"]:
+        assert T.sigmam(r, j) == pytest.approx(v, rel=1e-14)
+    for z, v in GOLD["lgr"]:
+        assert T.lgr(z) == pytest.approx(v, rel=1e-14)
+    for k, z, v in GOLD["P_k_nonlinear"]:
+        assert T.P_k_nonlinear(k, z) == pytest.approx(v, rel=1e-12)
+
+
+def test_limber_integrand_matches_reference_off_first_node(oracle_tables):
+    for ell, z, v in GOLD["limber_nodes"]:
+        assert oracle_tables.limber_integrand(ell, z) == pytest.approx(v, rel=1e-11, abs=1e-300)
+
+
+def test_first_node_clamp_is_deliberate(oracle_tables):
+    """The two lowest Gauss nodes (z ~ 4.7e-4, 2.5e-3) lie below half a table
+    bin, where the reference interpolates with table index -1 (an out-of-bounds
+    read, bispectrum.cu:356-359); the oracle clamps to bin 0, i.e. uses the
+    bin-0 values with total weight 1."""
+    a, _ = O.gq96()
+    low = [1.5 - 1.5 * x for x in a if (1.5 - 1.5 * x) / 3.0 * 256 < 0.5]
+    assert len(low) == 2
+    z0 = low[0]
+    arr = oracle_tables.arrays()
+    # with the clamp, the interpolated f_K at z0 is exactly bin 0's value
+    didx = z0 / 3.0 * 256
+    assert int(didx) == 0 and didx - int(didx) < 0.5
+    # integrand_bkappa at z0 with ell's away from the cut-offs is finite
+    v = oracle_tables.integrand_bkappa(z0, 100.0, 120.0, 150.0)
+    assert np.isfinite(v)
+
+
+def test_map3_with_reference_cubature(oracle_tables):
+    for rec in GOLD["map3_ref_cubature"]:
+        th = [x * O.ARCMIN for x in rec["theta_arcmin"]]
+        v, e, n = oracle_tables.map3(th)
+        assert v == pytest.approx(rec["value"], rel=1e-13)
+
+
+@pytest.mark.skipif(O.ref_lib() is None, reason="reference harness not built here")
+def test_oracle_cubature_bit_identical_to_reference():
+    L, R = O.lib(), O.ref_lib()
+
+    @O.INTEGRAND_V
+    def f(ndim, npts, x, fdata, fdim, fval):
+        for i in range(npts):
+            a, b = x[i * ndim], x[i * ndim + 1]
+            c = x[i * ndim + 2] if ndim > 2 else 0.0
+            fval[i * fdim] = math.exp(-50 * ((a - 0.3) ** 2 + (b - 0.6) ** 2 + (c - 0.2) ** 2)) + 0.1 * a * b
+            if fdim > 1:
+                fval[i * fdim + 1] = math.sin(3 * a) * b
+        return 0
+
+    for dim, fdim in ((2, 1), (3, 1), (3, 2)):
+        xmin, xmax = np.zeros(dim), np.ones(dim)
+        res = []
+        for fn in (L.orc_hcubature_v, R.ref_hcubature_v):
+            v, e = np.zeros(fdim), np.zeros(fdim)
+            fn(fdim, C.cast(f, C.c_void_p), None, dim, O._dp(xmin), O._dp(xmax), 0, 0, 1e-5, 3, O._dp(v), O._dp(e))
+            res.append((v.copy(), e.copy()))
+        assert np.array_equal(res[0][0], res[1][0]) and np.array_equal(res[0][1], res[1][1])
+
+
+def test_oracle_cubature_1d_gauss_kronrod():
+    L = O.lib()
+
+    @O.INTEGRAND_V
+    def f(ndim, npts, x, fdata, fdim, fval):
+        for i in range(npts):
+            fval[i] = math.exp(-x[i])
+        return 0
+
+    v, e = np.zeros(1), np.zeros(1)
+    L.orc_hcubature_v(1, C.cast(f, C.c_void_p), None, 1, O._dp(np.array([0.0])), O._dp(np.array([3.0])), 0, 0,
+                      1e-10, 3, O._dp(v), O._dp(e))
+    assert v[0] == pytest.approx(1 - math.exp(-3), rel=1e-12)
+
+
+def test_ogata_nodes_against_scipy_zeros():
+    sp = pytest.importorskip("scipy.special")
+    W = O.ogata_weights()
+    h = 0.1
+    for row, nu in ((0, 6), (2, 2)):
+        zeros = sp.jn_zeros(nu, 32)
+        xi = zeros / math.pi
+        psi = np.pi * (h * xi) * np.tanh(np.pi / 2 * np.sinh(h * xi)) / h
+        assert np.allclose(W[row, 1:], psi, rtol=1e-12)
+        Jn1 = sp.jv(nu + 1, zeros)
+        w = 2 / (np.pi * zeros * Jn1 ** 2)
+        t = h * xi
+        psip = (np.sinh(np.pi * np.sinh(t)) + np.pi * t * np.cosh(t)) / (np.cosh(np.pi * np.sinh(t)) + 1)
+        prod = w * psi ** 3 * sp.jv(nu, psi) * psip
+        # psi_k approaches the zeros of J_nu as k grows, so J_nu(psi_k) and the
+        # product weights fall towards zero and are conditioned in absolute terms
+        assert np.allclose(W[row + 1, 1:], prod, rtol=1e-10, atol=1e-10 * np.abs(prod).max())

@@ -1,0 +1,335 @@
+"""threepoint_gb300: GB300 (sm_103a) implementation of threepoint's model path.
+
+Python binding of the C ABI in ``include/threepoint_gb300.h`` (the library
+``threepoint_gb300/build/libthreepoint_gb300.so``), with the reference's API
+names: ``cosmology``, ``read_n_of_z``, ``read_thetas``,
+``convert_angle_to_rad``, ``set_cosmology``, ``MapMapMap``, ``gamma0..3``,
+``T1_total``/``T2_total``/``T4_total``.
+
+There is no CPU fallback: every numerical call runs the CUDA kernels of the
+shared library, and importing the numerical API without the built library
+raises ``RuntimeError``.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+import os
+from dataclasses import dataclass, fields
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "build", "libthreepoint_gb300.so")
+
+TP_OK, TP_ERR_ARG, TP_ERR_IO, TP_ERR_FORMAT, TP_ERR_CUDA, TP_ERR_STATE, TP_ERR_CAPACITY, TP_ERR_NOMEM = range(8)
+FP64, FP32 = 0, 1
+GEOM_CIRCLE, GEOM_SQUARE, GEOM_INFINITE = 0, 1, 2
+N_REDSHIFT_BINS = 256
+ARCMIN = 2.9088820866e-4
+
+
+class ThreepointError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__(f"status {status}: {msg}")
+        self.status = status
+
+
+class _Cosmo(C.Structure):
+    _fields_ = [(n, C.c_double) for n in ("h", "sigma8", "omb", "omc", "ns", "w", "om", "ow", "zmax")]
+
+
+@dataclass
+class cosmology:
+    """Cosmological parameters (cuda_version/cosmology.cuh:13-29)."""
+    h: float = 0.7
+    sigma8: float = 0.8
+    omb: float = 0.048
+    omc: float = 0.252
+    ns: float = 0.96
+    w: float = -1.0
+    om: float = 0.3
+    ow: float = 0.7
+    zmax: float = 3.0
+
+    @classmethod
+    def flat(cls, om, sigma8, h, w, ns, omb=0.048, zmax=3.0):
+        return cls(h=h, sigma8=sigma8, omb=omb, omc=om - omb, ns=ns, w=w, om=om, ow=1 - om, zmax=zmax)
+
+    @classmethod
+    def from_file(cls, path):
+        c = _Cosmo()
+        _check(None, lib().tp_cosmology_from_file(path.encode(), C.byref(c)))
+        return cls(**{f.name: getattr(c, f.name) for f in fields(cls)})
+
+    def _c(self):
+        return _Cosmo(**{f.name: float(getattr(self, f.name)) for f in fields(self)})
+
+
+_lib = None
+
+
+def lib():
+    """Load the shared library (raises if it has not been built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(f"{LIB_PATH} not built: run threepoint_gb300.build.build() or __graft_entry__.build()")
+        L = C.CDLL(LIB_PATH)
+        d, i, p, l = C.c_double, C.c_int, C.c_void_p, C.c_long
+        dp, ip, i64p = C.POINTER(C.c_double), C.POINTER(C.c_int), C.POINTER(C.c_int64)
+        L.tp_status_string.restype = C.c_char_p
+        L.tp_status_string.argtypes = [i]
+        L.tp_last_error.restype = C.c_char_p
+        L.tp_last_error.argtypes = [p]
+        L.tp_version.restype = C.c_char_p
+        L.tp_cosmology_from_file.argtypes = [C.c_char_p, C.POINTER(_Cosmo)]
+        L.tp_read_n_of_z.argtypes = [C.c_char_p, i, d, dp]
+        L.tp_rebin_n_of_z.argtypes = [dp, dp, i, i, d, dp]
+        L.tp_read_thetas.argtypes = [C.c_char_p, dp, i, ip]
+        L.tp_convert_angle_to_rad.argtypes = [d, C.c_char_p, dp]
+        L.tp_ctx_create.argtypes = [i, C.POINTER(p)]
+        L.tp_ctx_destroy.argtypes = [p]
+        L.tp_set_cosmologies.argtypes = [p, C.POINTER(_Cosmo), i, dp, i, dp, d, d, d]
+        L.tp_set_shape_noise.argtypes = [p, d, d, i]
+        L.tp_get_tables.argtypes = [p, i, dp]
+        L.tp_bkappa_batch.argtypes = [p, ip, dp, l, i, dp]
+        L.tp_pell_batch.argtypes = [p, i, dp, l, i, dp]
+        L.tp_map3_batch.argtypes = [p, ip, i, dp, i, d, d, d, d, d, i, dp, dp, i64p, ip]
+        L.tp_map3_jobs_device.argtypes = [p, p, p, i, d, d, d, d, d, i, p, p, p, p, p]
+        L.tp_ctx_stream.restype = p
+        L.tp_ctx_stream.argtypes = [p]
+        L.tp_pipe_peaks.argtypes = [i, dp]
+        L.tp_gamma_batch.argtypes = [p, i, dp, i, i, d, i, dp, ip]
+        L.tp_ogata_weights.argtypes = [dp]
+        L.tp_cov_total_batch.argtypes = [p, i, i, i, d, d, dp, dp, i, i, dp, ip]
+        _lib = L
+    return _lib
+
+
+def _check(ctx, st):
+    if st != TP_OK:
+        L = lib()
+        msg = L.tp_status_string(st).decode()
+        if ctx is not None:
+            detail = L.tp_last_error(ctx).decode()
+            if detail:
+                msg += ": " + detail
+        raise ThreepointError(st, msg)
+
+
+def _dp(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def _arr(x, dtype=np.float64):
+    return np.ascontiguousarray(x, dtype=dtype)
+
+
+# ---------------------------------------------------------------------------
+# inputs
+# ---------------------------------------------------------------------------
+def read_n_of_z(path, n_bins=N_REDSHIFT_BINS, zmax=3.0):
+    """cuda_version/helpers.cu:9-128"""
+    out = np.zeros(n_bins)
+    _check(None, lib().tp_read_n_of_z(str(path).encode(), n_bins, zmax, _dp(out)))
+    return out
+
+
+def rebin_n_of_z(zs, ns, n_bins=N_REDSHIFT_BINS, zmax=3.0):
+    """read_n_of_z's rebinning of an in-memory (z, n) table (helpers.cu:37-128)"""
+    zs, ns = _arr(zs), _arr(ns)
+    out = np.zeros(n_bins)
+    _check(None, lib().tp_rebin_n_of_z(_dp(zs), _dp(ns), len(zs), n_bins, zmax, _dp(out)))
+    return out
+
+
+def read_thetas(path, cap=4096):
+    """cuda_version/helpers.cu:176-200"""
+    out = np.zeros(cap)
+    n = C.c_int(0)
+    _check(None, lib().tp_read_thetas(str(path).encode(), _dp(out), cap, C.byref(n)))
+    return out[: min(n.value, cap)].copy()
+
+
+def convert_angle_to_rad(value, unit="arcmin"):
+    """cuda_version/helpers.cu:130-153"""
+    out = C.c_double(0)
+    _check(None, lib().tp_convert_angle_to_rad(float(value), unit.encode(), C.byref(out)))
+    return out.value
+
+
+def theta_triplets(thetas):
+    """theta1<=theta2<=theta3 combinations in the reference's loop order
+    (cuda_version/calculateApertureStatistics.cu:92-115)."""
+    n = len(thetas)
+    return [(thetas[i], thetas[j], thetas[k]) for i in range(n) for j in range(i, n) for k in range(j, n)]
+
+
+# ---------------------------------------------------------------------------
+class Context:
+    """One CUDA device + stream + the device tables of a batch of cosmologies."""
+
+    def __init__(self, device: int = 0):
+        self._h = C.c_void_p(0)
+        _check(None, lib().tp_ctx_create(device, C.byref(self._h)))
+        self.n_cosmo = 0
+        self.cosmologies = []
+
+    def close(self):
+        if self._h:
+            lib().tp_ctx_destroy(self._h)
+            self._h = C.c_void_p(0)
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # -- set_cosmology (cuda_version/bispectrum.cu:100-219), batched --------
+    def set_cosmologies(self, cosmos, nz, pk=None, dk=0.0, kmin=0.0, kmax=0.0):
+        cosmos = list(cosmos)
+        arr = (_Cosmo * len(cosmos))(*[c._c() for c in cosmos])
+        nz = _arr(nz)
+        stride = 0 if nz.ndim == 1 else N_REDSHIFT_BINS
+        if nz.size not in (N_REDSHIFT_BINS, N_REDSHIFT_BINS * len(cosmos)):
+            raise ValueError("nz must hold 256 values or 256 per cosmology")
+        pkp = None
+        if pk is not None:
+            pk = _arr(pk)
+            if pk.size != 256 * len(cosmos):
+                pk = np.tile(pk.reshape(-1)[:256], len(cosmos))
+            pkp = _dp(pk)
+        _check(self._h, lib().tp_set_cosmologies(self._h, arr, len(cosmos), _dp(nz), stride, pkp, dk, kmin, kmax))
+        self.n_cosmo = len(cosmos)
+        self.cosmologies = cosmos
+
+    def set_cosmology(self, cosmo, nz, pk=None, dk=0.0, kmin=0.0, kmax=0.0):
+        self.set_cosmologies([cosmo], nz, pk, dk, kmin, kmax)
+
+    def set_shape_noise(self, sigma_eps, n_gal_per_rad2, constant_powerspectrum=False):
+        _check(self._h, lib().tp_set_shape_noise(self._h, sigma_eps, n_gal_per_rad2, int(constant_powerspectrum)))
+
+    def tables(self, i=0):
+        out = np.zeros(6 * 256 + 1)
+        _check(self._h, lib().tp_get_tables(self._h, i, _dp(out)))
+        names = ("f_K", "g", "D1", "r_sigma", "n_eff", "ncur")
+        d = {n: out[k * 256:(k + 1) * 256].copy() for k, n in enumerate(names)}
+        d["norm"] = out[-1]
+        return d
+
+    # -- point evaluations ---------------------------------------------------
+    def bkappa(self, ell, cosmo_index=None, precision=FP64):
+        ell = _arr(ell).reshape(-1, 3)
+        out = np.zeros(len(ell))
+        ip = None
+        if cosmo_index is not None:
+            ci = _arr(np.broadcast_to(cosmo_index, (len(ell),)), np.int32)
+            ip = ci.ctypes.data_as(C.POINTER(C.c_int))
+        _check(self._h, lib().tp_bkappa_batch(self._h, ip, _dp(ell), len(ell), precision, _dp(out)))
+        return out
+
+    def Pell(self, ell, cosmo_index=0, precision=FP64):
+        ell = _arr(ell).reshape(-1)
+        out = np.zeros(len(ell))
+        _check(self._h, lib().tp_pell_batch(self._h, cosmo_index, _dp(ell), len(ell), precision, _dp(out)))
+        return out
+
+    # -- <Map^3> (cuda_version/apertureStatistics.cu:201-230) -------------
+    def map3_batch(self, thetas, cosmo_index=None, phiMin=0.0, phiMax=2 * math.pi, lMin=1.0, lMax=0.0,
+                   rel_tol=1e-4, precision=FP64, return_info=False, check=True):
+        th = _arr(thetas).reshape(-1, 3)
+        if cosmo_index is None:
+            cosmo_index = list(range(self.n_cosmo))
+        ci = _arr(cosmo_index, np.int32).reshape(-1)
+        nc, nt = len(ci), len(th)
+        out = np.zeros(nc * nt)
+        err = np.zeros(nc * nt)
+        nev = np.zeros(nc * nt, dtype=np.int64)
+        st = np.zeros(nc * nt, dtype=np.int32)
+        rc = lib().tp_map3_batch(self._h, ci.ctypes.data_as(C.POINTER(C.c_int)), nc, _dp(th), nt, phiMin, phiMax,
+                                 lMin, lMax, rel_tol, precision, _dp(out), _dp(err),
+                                 nev.ctypes.data_as(C.POINTER(C.c_int64)), st.ctypes.data_as(C.POINTER(C.c_int)))
+        if check or rc != TP_ERR_CAPACITY:
+            _check(self._h, rc)
+        out, err, nev, st = (a.reshape(nc, nt) for a in (out, err, nev, st))
+        if return_info:
+            return out, dict(err=err, neval=nev, status=st)
+        return out
+
+    def MapMapMap(self, thetas, phiMin=0.0, phiMax=2 * math.pi, lMin=1.0, precision=FP64, cosmo_index=0):
+        """<Map^3>(theta1, theta2, theta3) [rad] of one cosmology
+        (apertureStatistics.cuh:106)."""
+        return float(self.map3_batch([thetas], [cosmo_index], phiMin, phiMax, lMin, precision=precision)[0, 0])
+
+    def map3_jobs_device(self, job_cosmo, job_theta, out, err=None, neval=None, status=None, phiMin=0.0,
+                         phiMax=2 * math.pi, lMin=1.0, lMax=0.0, rel_tol=1e-4, precision=FP32, nlive=None):
+        """Asynchronous device-resident variant: arguments are torch CUDA
+        tensors (int32 [n], float64 [n,3], float64 [n] ...)."""
+        n = int(job_cosmo.numel())
+        ptr = lambda t: C.c_void_p(t.data_ptr()) if t is not None else None
+        _check(self._h, lib().tp_map3_jobs_device(self._h, ptr(job_cosmo), ptr(job_theta), n, phiMin, phiMax, lMin,
+                                                  lMax, rel_tol, precision, ptr(out), ptr(err), ptr(neval),
+                                                  ptr(nlive), ptr(status)))
+
+    @property
+    def stream_handle(self):
+        """The library stream of this context (an int cudaStream_t)."""
+        return lib().tp_ctx_stream(self._h)
+
+    # -- shear 3PCF (cuda_version/gamma.cu:98-148) ---------------------------
+    def gamma_batch(self, x, comp_mask=0xF, rel_tol=1e-3, precision=FP64, cosmo_index=0):
+        x = _arr(x).reshape(-1, 3)
+        out = np.zeros(len(x) * 8)
+        st = np.zeros(len(x), dtype=np.int32)
+        _check(self._h, lib().tp_gamma_batch(self._h, cosmo_index, _dp(x), len(x), comp_mask, rel_tol, precision,
+                                             _dp(out), st.ctypes.data_as(C.POINTER(C.c_int))))
+        o = out.reshape(-1, 4, 2)
+        return o[..., 0] + 1j * o[..., 1]
+
+    def gamma0(self, x1, x2, x3, **kw):
+        return complex(self.gamma_batch([(x1, x2, x3)], comp_mask=1, **kw)[0, 0])
+
+    def gamma1(self, x1, x2, x3, **kw):
+        return complex(self.gamma_batch([(x1, x2, x3)], comp_mask=2, **kw)[0, 1])
+
+    def gamma2(self, x1, x2, x3, **kw):
+        return complex(self.gamma_batch([(x1, x2, x3)], comp_mask=4, **kw)[0, 2])
+
+    def gamma3(self, x1, x2, x3, **kw):
+        return complex(self.gamma_batch([(x1, x2, x3)], comp_mask=8, **kw)[0, 3])
+
+    # -- covariance (cuda_version/apertureStatisticsCovariance.cu:272-683) --
+    def cov_total(self, term, th123, th456, geometry=GEOM_SQUARE, thetaMax=0.0, area=0.0, precision=FP64,
+                  cosmo_index=0):
+        a = _arr(th123).reshape(-1, 3)
+        b = _arr(th456).reshape(-1, 3)
+        out = np.zeros(len(a))
+        st = np.zeros(len(a), dtype=np.int32)
+        _check(self._h, lib().tp_cov_total_batch(self._h, cosmo_index, term, geometry, thetaMax, area, _dp(a), _dp(b),
+                                                 len(a), precision, _dp(out), st.ctypes.data_as(C.POINTER(C.c_int))))
+        return out
+
+
+def ogata_weights():
+    out = np.zeros(4 * 33)
+    _check(None, lib().tp_ogata_weights(_dp(out)))
+    return out.reshape(4, 33)
+
+
+def version():
+    return lib().tp_version().decode()
+
+
+def pipe_peaks(device=0):
+    """Measured whole-device throughput: (SFU ex2 ops/s, FP32 FMA/s, FP64 FMA/s)."""
+    out = np.zeros(3)
+    _check(None, lib().tp_pipe_peaks(device, _dp(out)))
+    return tuple(out)

@@ -1,0 +1,213 @@
+// BiHalofit bispectrum (Takahashi et al. 2020, Eqs. B4-B9) evaluated at one
+// fixed line-of-sight node from precomputed per-node coefficients; the same
+// formula as the reference's bispec (cuda_version/bispectrum.cu:221-291,
+// 602-719) with every z-only factor hoisted into the node table
+// (tp_tables.cu: k_node_coefs) and every triangle-shape factor (r1, r2,
+// F2_tree) hoisted into the per-point record. Templated on the arithmetic
+// type: double is the plain FP64 path; float uses the SFU approximations
+// ex2/lg2/rcp.approx and is summed with Kahan compensation by its callers.
+#pragma once
+#include "tp_internal.cuh"
+
+namespace tp {
+
+template <typename R>
+struct Mth;
+template <>
+struct Mth<float> {
+  static __device__ __forceinline__ float ex2(float x) {
+    float r;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+  }
+  static __device__ __forceinline__ float lg2(float x) {
+    float r;
+    asm("lg2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+  }
+  static __device__ __forceinline__ float rcp(float x) {
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+  }
+};
+template <>
+struct Mth<double> {
+  static __device__ __forceinline__ double ex2(double x) { return exp2(x); }
+  static __device__ __forceinline__ double lg2(double x) { return log2(x); }
+  static __device__ __forceinline__ double rcp(double x) { return 1.0 / x; }
+};
+
+// Cosmology constants of the integrands in arithmetic type R.
+template <typename R>
+struct CosmoK {
+  R omh2, sa, one_m_sa, sh043, theta2, l2theta2, c184, ehc, ns, alpha_max;
+  R l2h;             // log2(h)
+  int pk_given;
+  R ln_kmin, inv_dk;  // tabulated P(k)
+  const double* pk;   // 256 values (FP64, read through the cache)
+};
+
+template <typename R>
+__host__ __device__ inline CosmoK<R> make_cosmok(const EHConst& e, const CosmoDev& c, const double* pk_dev) {
+  CosmoK<R> k;
+  k.omh2 = (R)e.omh2;
+  k.sa = (R)e.sa;
+  k.one_m_sa = (R)e.one_m_sa;
+  k.sh043 = (R)(0.43 * e.sh);
+  k.theta2 = (R)e.theta2;
+  k.l2theta2 = (R)log2(e.theta2);
+  k.c184 = (R)e.c184;
+  k.ehc = (R)e.ehc;
+  k.ns = (R)e.ns;
+  k.alpha_max = (R)(1. - (2. / 3.) * c.ns);
+  k.l2h = (R)log2(c.h);
+  k.pk_given = c.pk_given;
+  k.ln_kmin = (R)(c.pk_given ? log(c.kmin) : 0.0);
+  k.inv_dk = (R)(c.pk_given ? 1.0 / c.dk : 0.0);
+  k.pk = pk_dev;
+  return k;
+}
+
+// Linear P(k) at kk = k*h [1/Mpc] with l2kk = log2(kk) (bispectrum.cu:602-693).
+template <typename R>
+__device__ __forceinline__ R plin(const CosmoK<R>& K, R kk, R l2kk) {
+  typedef Mth<R> M;
+  if (K.pk_given) {
+    // table in k [h/Mpc], linear interpolation in ln k
+    R lnk = (l2kk - K.l2h) * (R)LN2;
+    R didx = (lnk - K.ln_kmin) * K.inv_dk;
+    if (didx <= (R)0) return (R)K.pk[0];
+    if (didx >= (R)(NK - 1)) return (R)K.pk[NK - 1];
+    int idx = (int)didx;
+    R f = didx - (R)idx;
+    return (R)K.pk[idx] * ((R)1 - f) + (R)K.pk[idx + 1] * f;
+  }
+  R x = kk * K.sh043;
+  R x2 = x * x;
+  R geff = K.omh2 * (K.sa + K.one_m_sa * M::rcp((R)1 + x2 * x2));
+  R l2q = l2kk + K.l2theta2 - M::lg2(geff);
+  R qe = M::ex2(l2q);
+  R q111 = M::ex2((R)1.11 * l2q);
+  R L = (R)LN2 * M::lg2((R)2.718281828 + K.c184 * qe);
+  R C = (R)14.4 + (R)325.0 * M::rcp((R)1 + (R)60.5 * q111);
+  R r = L * M::rcp(L + C * qe * qe);
+  return K.ehc * M::ex2(K.ns * l2kk) * r * r;
+}
+
+// Triangle record shared by all nodes of one b_kappa evaluation.
+template <typename R>
+struct Tri {
+  R l[3];      // ell_i
+  R lg[3];     // log2 ell_i
+  R log2r1;    // log2(ell_min/ell_max)
+  R r2sq;      // r2^2, r2 = (ell_mid + ell_min - ell_max)/ell_max
+  R pr2;       // 10^(0.007 r2)
+  R f2t[3];    // F2_tree(1,2,3), F2_tree(2,3,1), F2_tree(3,1,2)
+};
+
+__host__ __device__ inline double f2_tree(double k1, double k2, double k3) {
+  double c12 = 0.5 * (k3 * k3 - k1 * k1 - k2 * k2) / (k1 * k2);
+  return (5. / 7.) + 0.5 * c12 * (k1 / k2 + k2 / k1) + (2. / 7.) * c12 * c12;
+}
+
+template <typename R>
+__device__ inline void make_tri(double l1, double l2, double l3, Tri<R>& T) {
+  T.l[0] = (R)l1;
+  T.l[1] = (R)l2;
+  T.l[2] = (R)l3;
+  T.lg[0] = (R)log2(l1);
+  T.lg[1] = (R)log2(l2);
+  T.lg[2] = (R)log2(l3);
+  double a = l1, b = l2, c = l3, t;
+  if (a < b) { t = a; a = b; b = t; }
+  if (a < c) { t = a; a = c; c = t; }
+  if (b < c) { t = b; b = c; c = t; }
+  // a >= b >= c (bispectrum.cu:235-247)
+  double r1 = c / a, r2 = (b + c - a) / a;
+  T.log2r1 = (R)log2(r1);
+  T.r2sq = (R)(r2 * r2);
+  T.pr2 = (R)exp2(LOG2_10 * 0.007 * r2);
+  T.f2t[0] = (R)f2_tree(l1, l2, l3);
+  T.f2t[1] = (R)f2_tree(l2, l3, l1);
+  T.f2t[2] = (R)f2_tree(l3, l1, l2);
+}
+
+// B(ell_i / f_K(z_j), z_j) for node j; nc points at the node table of the
+// cosmology (coef c of node j at nc[c*NNODE + j]).
+template <typename R>
+__device__ __forceinline__ R bispec_node(const R* __restrict__ nc, int j, const Tri<R>& T, const CosmoK<R>& K) {
+  typedef Mth<R> M;
+  const R s = nc[NC_S * NNODE + j], l2s = nc[NC_L2S * NNODE + j];
+  const R hf = nc[NC_HF * NNODE + j], l2hf = nc[NC_L2HF * NNODE + j];
+  R q[3], lq[3], P[3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    q[i] = T.l[i] * s;
+    lq[i] = T.lg[i] + l2s;
+  }
+  if (nc[NC_TREE * NNODE + j] != (R)0) {
+    // tree level for z > 10 (bispectrum.cu:229-230,695-698)
+#pragma unroll
+    for (int i = 0; i < 3; ++i) P[i] = plin<R>(K, T.l[i] * hf, T.lg[i] + l2hf);
+    return nc[NC_D1P4 * NNODE + j] * (R)2 *
+           (T.f2t[0] * P[0] * P[1] + T.f2t[1] * P[1] * P[2] + T.f2t[2] * P[2] * P[0]);
+  }
+  // 1-halo term (B4, B7)
+  const R an = M::ex2(nc[NC_ANA * NNODE + j] - nc[NC_ANR * NNODE + j] * M::ex2(nc[NC_ANC * NNODE + j] * T.log2r1));
+  R al = M::ex2(nc[NC_ALA * NNODE + j] + nc[NC_ALD * NNODE + j] * T.r2sq);
+  al = al > K.alpha_max ? K.alpha_max : al;
+  const R be = nc[NC_BETAB * NNODE + j] * T.pr2;
+  const R bn = nc[NC_BN * NNODE + j], cn = nc[NC_CN * NNODE + j];
+  R bs1h = (R)1;
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    R cq = cn * q[i];
+    bs1h *= cq * M::rcp((an * M::ex2(al * lq[i]) + bn * M::ex2(be * lq[i])) * (cq + (R)1));
+  }
+  // 3-halo term (B5, B6, B9)
+  const R fn = nc[NC_FN * NNODE + j], gn = nc[NC_GN * NNODE + j], hn = nc[NC_HN * NNODE + j];
+  const R mn = nc[NC_MN * NNODE + j], nn = nc[NC_NN * NNODE + j];
+  const R mun = nc[NC_MUN * NNODE + j], nun = nc[NC_NUN * NNODE + j];
+  const R pn = nc[NC_PN * NNODE + j], en = nc[NC_EN * NNODE + j];
+  const R d1sq = nc[NC_D1SQ * NNODE + j];
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    R qi = q[i];
+    R a = ((R)1 + fn * qi * qi) * M::rcp((R)1 + gn * qi + hn * qi * qi) * d1sq *
+          plin<R>(K, T.l[i] * hf, T.lg[i] + l2hf);
+    R x = pn * qi;
+    R x3 = x * x * x;
+    R mq = mn * M::ex2(mun * lq[i]) + nn * M::ex2(nun * lq[i]);
+    P[i] = a + x3 * M::rcp(mq * (x3 + (R)1));
+  }
+  const R dn = nc[NC_DN * NNODE + j];
+  R bs3h = (R)2 * ((T.f2t[0] + dn * q[2]) * P[0] * P[1] + (T.f2t[1] + dn * q[0]) * P[1] * P[2] +
+                   (T.f2t[2] + dn * q[1]) * P[2] * P[0]);
+  bs3h *= M::rcp(((R)1 + en * q[0]) * ((R)1 + en * q[1]) * ((R)1 + en * q[2]));
+  return bs1h + bs3h;
+}
+
+__device__ __forceinline__ double uhat(double eta) {
+  double t = 0.5 * eta * eta;
+  return t * exp(-t);
+}
+
+// Kahan accumulator
+template <typename R>
+struct KSum {
+  R s = 0, c = 0;
+  __device__ __forceinline__ void add(R v) {
+    R y = v - c;
+    R t = s + y;
+    c = (t - s) - y;
+    s = t;
+  }
+};
+template <>
+struct KSum<double> {
+  double s = 0;
+  __device__ __forceinline__ void add(double v) { s += v; }
+};
+
+}  // namespace tp

@@ -1,0 +1,51 @@
+// Context object behind the opaque tp_ctx handle (host side).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "tp_internal.cuh"
+
+struct tp_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::string err;
+  int max_ctas = 0;  // 0 = all resident CTAs
+
+  // cosmologies and their device tables
+  int n_cosmo = 0;
+  int cosmo_cap = 0;
+  size_t nz_cap = 0;
+  std::vector<tp::CosmoDev> h_cos;
+  tp::CosmoDev* d_cos = nullptr;
+  tp::EHConst* d_eh = nullptr;
+  tp::TablesDev* d_tab = nullptr;
+  double* d_nz = nullptr;
+  double* d_ncoef64 = nullptr;
+  float* d_ncoef32 = nullptr;
+  double* d_hcoef = nullptr;
+  double* d_wscale64 = nullptr;
+  double* d_wscale32 = nullptr;
+  void* d_ck64 = nullptr;
+  void* d_ck32 = nullptr;
+
+  // shape noise of P(ell)
+  double sigma_eps = 0.0, ngal = 1.0;
+  int constant_ps = 0;
+
+  // scratch: per-CTA region stores; io: staging of host-API inputs/outputs
+  char* d_scratch = nullptr;
+  size_t scratch_bytes = 0;
+  char* d_io = nullptr;
+  size_t io_bytes = 0;
+  int* d_counter = nullptr;
+  unsigned* d_diag = nullptr;
+
+  void free_cosmo();
+  int ensure_scratch(size_t bytes);
+  int ensure_io(size_t bytes);
+};
+
+int tp_fail(tp_ctx* ctx, int st, const std::string& msg);
+int tp_cuda(tp_ctx* ctx, cudaError_t e, const char* where);

@@ -1,0 +1,99 @@
+// Internal declarations shared by the CUDA translation units of
+// libthreepoint_gb300.so. Nothing here is part of the public C ABI.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/threepoint_gb300.h"
+
+namespace tp {
+
+constexpr int NZ = 256;          // redshift bins of the tables (n_redshift_bins)
+constexpr int NK = 256;          // k bins of a tabulated linear P(k) (n_kbins)
+constexpr int NNODE = 96;        // Gauss-Legendre nodes of every line-of-sight integral
+constexpr double EPS = 1.0e-4;   // accuracy of the sigma(R)/growth iterations
+constexpr double H0_OVER_C = 100. / 299792.;
+constexpr double C_OVER_H0 = 2997.92;
+constexpr double PI = 3.14159265358979323846;
+constexpr double LOG2_10 = 3.32192809488736234787;
+constexpr double LN2 = 0.69314718055994530942;
+
+// Per-cosmology parameter block as uploaded to the device.
+struct CosmoDev {
+  double h, sigma8, omb, omc, ns, w, om, ow, zmax;
+  int pk_given;
+  double dk, kmin, kmax;
+  double sigma_eps, ngal;  // shape noise for the power spectrum (covariance)
+  int constant_ps;
+};
+
+// Eisenstein & Hu no-wiggle constants hoisted out of linear_pk
+// (the cosmology-only part of cuda_version/bispectrum.cu:651-680).
+struct EHConst {
+  double h, omh2, theta2, sa, one_m_sa, sh, c184, ehc, ns;
+};
+
+// FP64 z-tables of one cosmology (set_cosmology output), row layout
+// [f_K, g, D1, r_sigma, n_eff, ncur] x 256, then norm and dz.
+struct TablesDev {
+  double f_K[NZ], g[NZ], D1[NZ], r_sigma[NZ], n_eff[NZ], ncur[NZ];
+  double pk[NK];
+  double norm, dz;
+};
+
+// Per-node BiHalofit coefficients for the fixed line-of-sight nodes of
+// b_kappa: everything in bispec() that depends on z only, precomputed once
+// per cosmology. Stored structure-of-arrays: coef[c * NNODE + node].
+enum NodeCoef {
+  NC_W = 0,    // LOS weight: gauss w * dz/2 * 27/8 Om^3 (H0/c)^5 * (g(1+z))^3 / f_K / E
+  NC_S,        // r_sigma / f_K            (q = ell * S)
+  NC_L2S,      // log2(r_sigma / f_K)
+  NC_HF,       // h / f_K                  (k[1/Mpc] = ell * HF)
+  NC_L2HF,     // log2(h / f_K)
+  NC_ANA,      // log2(10) * (-2.167 - 2.944 ls - 1.106 ls^2 - 2.865 ls^3)
+  NC_ANR,      // 0.310 * log2(10)
+  NC_ANC,      // 10^(0.182 + 0.57 n_eff)
+  NC_BN, NC_CN,
+  NC_ALA,      // log2(10) * (-4.348 - 3.006 n - 0.5745 n^2)
+  NC_ALD,      // log2(10) * 10^(-0.9 + 0.2 n)
+  NC_BETAB,    // 10^(-1.731 - 2.845 n - 1.4995 n^2 - 0.2811 n^3)
+  NC_FN, NC_GN, NC_HN, NC_MN, NC_NN, NC_MUN, NC_NUN, NC_PN, NC_EN,
+  NC_DN,       // 10^(-0.483 + 0.892 ls - 0.086 Om(z)) (F2 correction)
+  NC_D1SQ,     // D1^2
+  NC_TREE,     // 1 when z > 10 (tree-level bispectrum), else 0
+  NC_D1P4,     // D1^4 (tree level)
+  NC_COUNT
+};
+
+// Per-node Halofit coefficients for the P_kappa line-of-sight integral
+// (P_k_nonlinear + limber prefactor at the fixed nodes; z-only parts).
+enum HaloCoef {
+  HC_W = 0,    // gauss w * dz/2 * 9/4 (H0/c)^3 Om^2 (1+z)^2 g^2 / E   (0 below z=1e-5)
+  HC_INVFK,    // 1/f_K
+  HC_RS,       // r_sigma
+  HC_D1SQ,     // D1^2
+  HC_A, HC_B, HC_C, HC_GAM, HC_ALPHA, HC_BETA, HC_XNU,
+  HC_F1, HC_F2, HC_F3,
+  HC_COUNT
+};
+
+
+// ---- helpers shared by several translation units ---------------------------
+__host__ __device__ inline double eh_linear_pk(const EHConst& e, double k) {
+  double kk = k * e.h;
+  double x = 0.43 * kk * e.sh;
+  double x2 = x * x;
+  double geff = e.omh2 * (e.sa + e.one_m_sa / (1.0 + x2 * x2));
+  double qeff = kk / geff * e.theta2;
+  double L = log(2.718281828 + e.c184 * qeff);
+  double C = 14.4 + 325.0 / (1.0 + 60.5 * pow(qeff, 1.11));
+  double r = L / (L + C * qeff * qeff);
+  return e.ehc * pow(kk, e.ns) * r * r;
+}
+
+EHConst make_eh_const(const CosmoDev& c, double norm);
+
+// host-side 96-point Gauss-Legendre rule on [-1,1] (positive half, ascending)
+void gauss_legendre96(double* a48, double* w48);
+
+}  // namespace tp

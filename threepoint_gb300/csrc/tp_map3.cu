@@ -1,0 +1,281 @@
+// <Map^3> integrand and its batched adaptive integration.
+//
+// Reference: integrand_Map3_kernel (cuda_version/apertureStatistics.cu:138-153),
+// MapMapMap (:201-230), bkappa / GQ96_of_bdelta / integrand_bkappa
+// (cuda_version/bispectrum.cu:293-333), uHat (apertureStatistics.cu:18-22).
+//
+// One integral = one (cosmology, theta-triplet) job. Point record: the
+// triangle (ell1, ell2, ell3), its shape factors and the outer factor
+// l1 l2 uHat(l1 t1) uHat(l2 t2) uHat(l3 t3); the 96 line-of-sight nodes of
+// b_kappa are split into G groups of 96/G nodes, one (point, group) item per
+// thread. The node table of the job's cosmology (NC_COUNT x 96) is staged in
+// shared memory with a bulk async copy when the CTA switches cosmology.
+#include <cuda_runtime.h>
+
+#include "tp_bispec.cuh"
+#include "tp_cubature.cuh"
+#include "tp_internal.cuh"
+#include "tp_kernels.cuh"
+
+namespace tp {
+
+template <typename R>
+struct Map3Policy {
+  static constexpr int G = 8;              // node groups per point
+  static constexpr int NPG = NNODE / G;    // nodes per group
+  static constexpr int CH = 8;             // regions per evaluation chunk
+  struct Rec {
+    Tri<R> tri;
+    double outer;  // l1 l2 uHat uHat uHat * node-weight scale
+    int live;
+  };
+  static constexpr int REC = (int)sizeof(Rec);
+  static constexpr size_t PSMEM = sizeof(R) * NC_COUNT * NNODE + sizeof(CosmoK<R>) + sizeof(BulkBar) + 128;
+
+  // inputs
+  const int* job_cosmo;
+  const double* job_theta;
+  const R* node_coef;        // [n_cosmo][NC_COUNT][NNODE] (weights normalised, see wscale)
+  const double* wscale;      // [n_cosmo]
+  const CosmoK<R>* ck;       // [n_cosmo]
+  double lmin, lmax, phimin, phimax;
+  // outputs
+  double* out;
+  double* err;
+  int64_t* neval;
+  int64_t* nlive;
+  int* status;
+  unsigned* diag;
+  // per-CTA state
+  R* s_nc;
+  CosmoK<R>* s_ck;
+  int cur_cosmo;
+  double th[3];
+  double scale;
+
+  __device__ BulkBar* bar(char* psmem) {
+    return (BulkBar*)(psmem + sizeof(R) * NC_COUNT * NNODE + ((sizeof(CosmoK<R>) + 15) & ~size_t(15)));
+  }
+  __device__ unsigned long long* live_counter(char* psmem) {
+    return (unsigned long long*)((char*)bar(psmem) + ((sizeof(BulkBar) + 15) & ~size_t(15)));
+  }
+  unsigned long long* s_live;
+
+  __device__ void begin_job(int job, char* psmem, double* xmin, double* xmax) {
+    s_nc = (R*)psmem;
+    s_ck = (CosmoK<R>*)(psmem + sizeof(R) * NC_COUNT * NNODE);
+    const int c = job_cosmo[job];
+    if (c != cur_cosmo) {
+      __syncthreads();
+      const R* src = node_coef + (size_t)c * NC_COUNT * NNODE;
+      constexpr int nbytes = (int)(sizeof(R) * NC_COUNT * NNODE);
+      static_assert(nbytes % 16 == 0, "bulk copy size must be a multiple of 16 bytes");
+      if (threadIdx.x == 0) {
+        // the node table (10-20 KB) is staged by one bulk async copy
+        if (!bulk_copy_g2s(bar(psmem), s_nc, src, nbytes)) {
+          for (int i = 0; i < NC_COUNT * NNODE; ++i) s_nc[i] = src[i];
+        }
+        *s_ck = ck[c];
+      }
+      __syncthreads();
+      cur_cosmo = c;
+    }
+    th[0] = job_theta[3 * job];
+    th[1] = job_theta[3 * job + 1];
+    th[2] = job_theta[3 * job + 2];
+    double tmin = fmin(th[0], fmin(th[1], th[2]));
+    double lm = lmax > 0 ? lmax : 10. / tmin;
+    xmin[0] = lmin;
+    xmin[1] = lmin;
+    xmin[2] = phimin;
+    xmax[0] = lm;
+    xmax[1] = lm;
+    xmax[2] = phimax;
+    scale = wscale[c];
+    s_live = live_counter(psmem);
+    if (threadIdx.x == 0) *s_live = 0ull;
+    __syncthreads();
+  }
+
+  __device__ void setup(int p, const double* x, char* recp) {
+    (void)p;
+    Rec& r = *(Rec*)recp;
+    double l1 = x[0], l2 = x[1], phi = x[2];
+    double s = l1 * l1 + l2 * l2 + 2 * l1 * l2 * cos(phi);
+    double l3 = s > 0 ? sqrt(s) : 0.0;
+    double outer = l1 * l2 * uhat(l1 * th[0]) * uhat(l2 * th[1]) * uhat(l3 * th[2]);
+    bool live = !(l1 == 0 || l2 == 0 || l3 == 0) && l1 > 1.0e-10 && l2 > 1.0e-10 && l3 > 1.0e-10 && outer != 0.0;
+    r.live = live;
+    r.outer = outer * scale;
+    if (live) {
+      make_tri<R>(l1, l2, l3, r.tri);
+      if (nlive) atomicAdd(s_live, 1ull);
+    }
+  }
+
+  __device__ void group(const char* recp, int g, double* pv) {
+    const Rec& r = *(const Rec*)recp;
+    if (!r.live) {
+      pv[0] = 0;
+      return;
+    }
+    const CosmoK<R> K = *s_ck;
+    KSum<R> acc;
+    const int j0 = g * NPG;
+#pragma unroll 1
+    for (int j = j0; j < j0 + NPG; ++j) {
+      R b = bispec_node<R>(s_nc, j, r.tri, K);
+      R v = s_nc[NC_W * NNODE + j] * b;
+      if (v != v) v = (R)0;  // NaN in bispec -> 0 (bispectrum.cu:327-331)
+      acc.add(v);
+    }
+    pv[0] = (double)acc.s;
+  }
+
+  __device__ void finalize(const char* recp, const double* sum, double* fv) {
+    const Rec& r = *(const Rec*)recp;
+    fv[0] = r.live ? r.outer * sum[0] : 0.0;
+  }
+
+  __device__ void end_job(int job, const double* V, const double* E, long long nev, int st) {
+    if (threadIdx.x == 0) {
+      const double norm = 1. / 8 / PI / PI / PI;
+      out[job] = V[0] * norm;
+      if (err) err[job] = E[0] * norm;
+      if (neval) neval[job] = nev;
+      if (nlive) nlive[job] = (int64_t)*s_live;
+      if (status) status[job] = st;
+    }
+  }
+};
+
+template <typename R, int NT>
+__global__ void __launch_bounds__(NT) k_map3(Map3Policy<R> pol_in, int njobs, int* job_counter, EngineCfg cfg,
+                                             char* scratch, size_t slot_bytes) {
+  Map3Policy<R> pol = pol_in;
+  pol.cur_cosmo = -1;
+  extern __shared__ __align__(16) char smem_[];
+  BulkBar* b = pol.bar(smem_);
+  if (threadIdx.x == 0) bulkbar_init(b);
+  __syncthreads();
+  adaptive_body<3, 1, NT, Map3Policy<R>>(pol, njobs, job_counter, cfg, scratch, slot_bytes);
+  if (threadIdx.x == 0 && b->timeouts && pol.diag) atomicAdd(pol.diag, b->timeouts);
+}
+
+template <typename R>
+size_t map3_smem_bytes() {
+  typedef Map3Policy<R> P;
+  constexpr int NP = GMRule<3>::NP;
+  size_t b = (P::PSMEM + 15) & ~size_t(15);
+  b += ((size_t)P::CH * NP * P::REC + 15) & ~size_t(15);
+  b += sizeof(double) * (size_t)P::G * P::CH * NP;
+  b += sizeof(double) * (size_t)P::CH * NP;
+  b += sizeof(EngineShared<1>) + 16;
+  return b;
+}
+
+// ---------------------------------------------------------------------------
+// Point evaluation of b_kappa (no cubature): one warp per point, 3 nodes per
+// lane, shuffle reduction.
+template <typename R>
+__global__ void k_bkappa_points(const int* cosmo_idx, const double* ell, long n, const R* node_coef,
+                                const double* wscale, const CosmoK<R>* ck, double* out) {
+  long w = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  int lane = threadIdx.x & 31;
+  if (w >= n) return;
+  int c = cosmo_idx ? cosmo_idx[w] : 0;
+  double l1 = ell[3 * w], l2 = ell[3 * w + 1], l3 = ell[3 * w + 2];
+  if (l1 == 0 || l2 == 0 || l3 == 0 || !(l1 > 1e-10 && l2 > 1e-10 && l3 > 1e-10)) {
+    if (lane == 0) out[w] = 0.0;
+    return;
+  }
+  Tri<R> T;
+  make_tri<R>(l1, l2, l3, T);
+  const R* nc = node_coef + (size_t)c * NC_COUNT * NNODE;
+  const CosmoK<R> K = ck[c];
+  KSum<R> acc;
+  for (int j = lane; j < NNODE; j += 32) {
+    R v = nc[NC_W * NNODE + j] * bispec_node<R>(nc, j, T, K);
+    if (v != v) v = (R)0;
+    acc.add(v);
+  }
+  double s = (double)acc.s;
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if (lane == 0) out[w] = s * wscale[c];
+}
+
+// ---------------------------------------------------------------------------
+constexpr int MAP3_NT = 256;
+
+template <typename R>
+static cudaError_t plan_map3_t(int njobs, int cap, int max_ctas, int* grid, size_t* smem, size_t* scratch) {
+  *smem = map3_smem_bytes<R>();
+  cudaError_t e =
+      cudaFuncSetAttribute(k_map3<R, MAP3_NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)*smem);
+  if (e != cudaSuccess) return e;
+  int dev = 0, sms = 0, per_sm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_map3<R, MAP3_NT>, MAP3_NT, *smem);
+  if (e != cudaSuccess) return e;
+  if (per_sm < 1) return cudaErrorInvalidConfiguration;
+  int g = sms * per_sm;
+  if (max_ctas > 0 && g > max_ctas) g = max_ctas;
+  if (g > njobs) g = njobs;
+  if (g < 1) g = 1;
+  *grid = g;
+  *scratch = (size_t)g * Slot<3, 1>::bytes(cap);
+  return cudaSuccess;
+}
+
+cudaError_t plan_map3(int precision, int njobs, int cap, int max_ctas, int* grid, size_t* smem, size_t* scratch) {
+  return precision == TP_FP64 ? plan_map3_t<double>(njobs, cap, max_ctas, grid, smem, scratch)
+                              : plan_map3_t<float>(njobs, cap, max_ctas, grid, smem, scratch);
+}
+
+template <typename R>
+static cudaError_t launch_map3_t(const Map3Launch& L, int grid, size_t smem, char* scratch, cudaStream_t st) {
+  cudaError_t e = cudaMemsetAsync(L.job_counter, 0, sizeof(int), st);
+  if (e != cudaSuccess) return e;
+  Map3Policy<R> pol;
+  pol.job_cosmo = L.job_cosmo;
+  pol.job_theta = L.job_theta;
+  pol.node_coef = (const R*)(sizeof(R) == 8 ? (const void*)L.ncoef64 : (const void*)L.ncoef32);
+  pol.wscale = sizeof(R) == 8 ? L.wscale64 : L.wscale32;
+  pol.ck = (const CosmoK<R>*)(sizeof(R) == 8 ? L.ck64 : L.ck32);
+  pol.lmin = L.lmin;
+  pol.lmax = L.lmax;
+  pol.phimin = L.phimin;
+  pol.phimax = L.phimax;
+  pol.out = L.out;
+  pol.err = L.err;
+  pol.neval = L.neval;
+  pol.nlive = L.nlive;
+  pol.status = L.status;
+  pol.diag = L.diag;
+  EngineCfg cfg{0.0, L.rel_tol, TP_NORM_L1, L.cap, L.max_sweeps};
+  size_t slot = Slot<3, 1>::bytes(L.cap);
+  k_map3<R, MAP3_NT><<<grid, MAP3_NT, smem, st>>>(pol, L.njobs, L.job_counter, cfg, scratch, slot);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_map3(const Map3Launch& L, int grid, size_t smem, char* scratch, cudaStream_t st) {
+  return L.precision == TP_FP64 ? launch_map3_t<double>(L, grid, smem, scratch, st)
+                                : launch_map3_t<float>(L, grid, smem, scratch, st);
+}
+
+cudaError_t launch_bkappa_points(int precision, const int* cosmo_idx, const double* ell, long n, const void* ncoef,
+                                 const double* wscale, const void* ck, double* out, cudaStream_t st) {
+  long threads = n * 32;
+  int bs = 256;
+  unsigned grid = (unsigned)((threads + bs - 1) / bs);
+  if (precision == TP_FP64)
+    k_bkappa_points<double><<<grid, bs, 0, st>>>(cosmo_idx, ell, n, (const double*)ncoef, wscale,
+                                                  (const CosmoK<double>*)ck, out);
+  else
+    k_bkappa_points<float><<<grid, bs, 0, st>>>(cosmo_idx, ell, n, (const float*)ncoef, wscale,
+                                                 (const CosmoK<float>*)ck, out);
+  return cudaGetLastError();
+}
+
+}  // namespace tp

@@ -1,0 +1,464 @@
+// GPU builder of the per-cosmology FP64 tables (the reference's host-side
+// set_cosmology, cuda_version/bispectrum.cu:100-219) and of the per-node
+// line-of-sight coefficients used by the integrand kernels.
+//
+// Layout in HBM: one TablesDev (~14 KB) per cosmology; one NC_COUNT x 96
+// double block (+ a float copy) of b_kappa node coefficients and one
+// HC_COUNT x 96 double block of Halofit node coefficients per cosmology.
+#include <math.h>
+
+#include "tp_bispec.cuh"
+#include "tp_internal.cuh"
+#include "tp_tables.cuh"
+
+namespace tp {
+
+__constant__ double c_gq_a[48];  // Gauss-Legendre abscissae on (0,1), ascending
+__constant__ double c_gq_w[48];
+
+// ---------------------------------------------------------------------------
+// host helpers
+// ---------------------------------------------------------------------------
+void gauss_legendre96(double* a48, double* w48) {
+  const int n = 96;
+  for (int i = 0; i < 48; ++i) {
+    long double x = cosl(3.14159265358979323846264338327950288L * (48 - i - 0.25L) / (n + 0.5L));
+    long double dp = 0;
+    for (int it = 0; it < 100; ++it) {
+      long double p0 = 1, p1 = x;
+      for (int k = 2; k <= n; ++k) {
+        long double p2 = ((2 * k - 1) * x * p1 - (k - 1) * p0) / k;
+        p0 = p1;
+        p1 = p2;
+      }
+      dp = n * (x * p1 - p0) / (x * x - 1);
+      long double dx = p1 / dp;
+      x -= dx;
+      if (fabsl(dx) < 1e-19L) break;
+    }
+    long double p0 = 1, p1 = x;
+    for (int k = 2; k <= n; ++k) {
+      long double p2 = ((2 * k - 1) * x * p1 - (k - 1) * p0) / k;
+      p0 = p1;
+      p1 = p2;
+    }
+    dp = n * (x * p1 - p0) / (x * x - 1);
+    a48[i] = (double)x;
+    w48[i] = (double)(2.0L / ((1 - x * x) * dp * dp));
+  }
+}
+
+// cosmology-only part of the Eisenstein & Hu fit (bispectrum.cu:651-686)
+EHConst make_eh_const(const CosmoDev& c, double norm) {
+  EHConst e;
+  double fc = c.omc / c.om, fb = c.omb / c.om;
+  double theta = 2.728 / 2.7;
+  double pc = 0.25 * (5.0 - sqrt(1.0 + 24.0 * fc));
+  double omh2 = c.om * c.h * c.h, ombh2 = c.omb * c.h * c.h;
+  double zeq = 2.5e+4 * omh2 / pow(theta, 4);
+  double b1 = 0.313 * pow(omh2, -0.419) * (1.0 + 0.607 * pow(omh2, 0.674));
+  double b2 = 0.238 * pow(omh2, 0.223);
+  double zd = 1291.0 * pow(omh2, 0.251) / (1.0 + 0.659 * pow(omh2, 0.828)) * (1.0 + b1 * pow(ombh2, b2));
+  double yd = (1.0 + zeq) / (1.0 + zd);
+  double sh = 44.5 * log(9.83 / omh2) / sqrt(1.0 + 10.0 * pow(ombh2, 0.75));
+  double alnu = fc * (5.0 - 2.0 * pc) / 5.0 * (1.0 - 0.553 * fb + 0.126 * fb * fb * fb) * pow(1.0 + yd, -pc) *
+                (1.0 + 0.5 * pc * (1.0 + 1.0 / (7.0 * (3.0 - 4.0 * pc))) / (1.0 + yd));
+  e.h = c.h;
+  e.omh2 = omh2;
+  e.theta2 = theta * theta;
+  e.sa = sqrt(alnu);
+  e.one_m_sa = 1.0 - e.sa;
+  e.sh = sh;
+  e.c184 = 1.84 * e.sa / (1.0 - 0.949 * fb);
+  // P(k) [h^-3 Mpc^3] = h^3 2 pi^2 norm^2 (2997.9/h)^(3+ns) * kk^ns * (L/(L+C q^2))^2
+  e.ehc = c.h * c.h * c.h * 2.0 * PI * PI * norm * norm * pow(2997.9 / c.h, 3. + c.ns);
+  e.ns = c.ns;
+  return e;
+}
+
+// ---------------------------------------------------------------------------
+// device FP64 physics of the table build
+// ---------------------------------------------------------------------------
+__device__ inline double d_E(const CosmoDev& c, double z) {
+  return sqrt(c.om * pow(1 + z, 3.0) + c.ow * pow(1 + z, 3 * (1.0 + c.w)));
+}
+
+// linear_pk, bispectrum.cu:602-693 (table branch or hoisted Eisenstein & Hu)
+__device__ inline double d_linear_pk(const CosmoDev& c, const EHConst& e, const double* pk, double k) {
+  if (c.pk_given) {
+    if (k >= c.kmax) return pk[NK - 1];
+    if (k <= c.kmin) return pk[0];
+    double didx = log(k / c.kmin) / c.dk;
+    int idx = (int)didx;
+    didx -= idx;
+    if (idx >= NK - 1) return pk[NK - 1];
+    return pk[idx] * (1 - didx) + pk[idx + 1] * didx;
+  }
+  return eh_linear_pk(e, k);
+}
+
+// window functions, bispectrum.cu:854-868
+__device__ inline double d_window(double x, int i) {
+  if (i == 0) return 3.0 / (x * x * x) * (sin(x) - x * cos(x));
+  if (i == 1) return exp(-0.5 * x * x);
+  if (i == 2) return x * exp(-0.5 * x * x);
+  if (i == 3) return x * x * (1 - x * x) * exp(-x * x);
+  return (3 * (x * x - 3) * sin(x) + 9 * x * cos(x)) / x / x / x / x;
+}
+
+__device__ inline double sigma_integrand(const CosmoDev& c, const EHConst& e, const double* pk, double k, double r,
+                                         int j) {
+  double w = d_window(k * r, j);
+  return k * k * k * d_linear_pk(c, e, pk, k) * (j < 3 ? w * w : w);
+}
+
+// sigma(R): nested doubling trapezoid in ln k (bispectrum.cu:796-852). All 32
+// lanes of the calling warp cooperate on the trapezoid sums and return the
+// same value (xor-butterfly sums are bitwise identical in every lane).
+__device__ double warp_sigmam(const CosmoDev& c, const EHConst& e, const double* pk, double r, int j) {
+  if (c.sigma8 < 1e-8) return 0;
+  const int lane = threadIdx.x & 31;
+  double k1 = 2. * PI / r, k2 = 2. * PI / r;
+  double xx = 0, xxpp = -1.0;
+  // iteration caps: at most 2^22 trapezoid points per pass; a non-finite sum
+  // (only for invalid cosmologies) ends the iteration
+  for (int outer = 0; outer < 40; ++outer) {
+    k1 = k1 / 10.0;
+    k2 = k2 * 2.0;
+    double a = log(k1), b = log(k2);
+    double xxp = -1.0;
+    int n = 2;
+    double ends = 0.5 * (sigma_integrand(c, e, pk, k1, r, j) + sigma_integrand(c, e, pk, k2, r, j));
+    for (int inner = 0; inner < 21; ++inner) {
+      n = n * 2;
+      double hh = (b - a) / (double)n;
+      double part = 0;
+      for (int i = 1 + lane; i < n; i += 32) part += sigma_integrand(c, e, pk, exp(a + hh * i), r, j);
+      for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
+      xx = (part + ends) * hh;
+      if (!isfinite(xx) || fabs((xx - xxp) / xx) < EPS) break;
+      xxp = xx;
+    }
+    if (!isfinite(xx) || fabs((xx - xxpp) / xx) < EPS) break;
+    xxpp = xx;
+  }
+  if (j < 3) return sqrt(xx / (2.0 * PI * PI));
+  return xx / (2.0 * PI * PI);
+}
+
+// growth ODE, bispectrum.cu:726-794
+__device__ inline double d_lgr_rhs(const CosmoDev& c, double la, double y0, double y1) {
+  double a = exp(la);
+  double ap = pow(a, -3. * c.w);
+  double g = -0.5 * (5. * c.om + (5. - 3 * c.w) * c.ow * ap) * y1 - 1.5 * (1. - c.w) * c.ow * ap * y0;
+  return g / (c.om + c.ow * ap);
+}
+__device__ double d_lgr(const CosmoDev& c, double z) {
+  double a = 1. / (1. + z), a0 = 1. / 1100.;
+  double yp = -1., y0 = 1, y1 = 0;
+  int n = 10;
+  for (int it = 0; it < 20; ++it) {  // at most 10*2^20 RK4 steps
+    n *= 2;
+    double h = (log(a) - log(a0)) / n;
+    double x = log(a0);
+    y0 = 1.;
+    y1 = 0.;
+    for (int i = 0; i < n; i++) {
+      double k10 = h * y1, k11 = h * d_lgr_rhs(c, x, y0, y1);
+      double a0_ = y0 + 0.5 * k10, a1_ = y1 + 0.5 * k11;
+      double k20 = h * a1_, k21 = h * d_lgr_rhs(c, x + 0.5 * h, a0_, a1_);
+      double b0_ = y0 + 0.5 * k20, b1_ = y1 + 0.5 * k21;
+      double k30 = h * b1_, k31 = h * d_lgr_rhs(c, x + 0.5 * h, b0_, b1_);
+      double c0_ = y0 + k30, c1_ = y1 + k31;
+      double k40 = h * c1_, k41 = h * d_lgr_rhs(c, x + h, c0_, c1_);
+      y0 += (k10 + k40) / 6. + (k20 + k30) / 3.;
+      y1 += (k11 + k41) / 6. + (k21 + k31) / 3.;
+      x += h;
+    }
+    if (!isfinite(y0) || fabs(y0 / yp - 1.) < 0.1 * EPS) break;
+    yp = y0;
+  }
+  return a * y0;
+}
+
+// ---------------------------------------------------------------------------
+// kernels
+// ---------------------------------------------------------------------------
+
+// norm = sigma8 / sigma(8 Mpc/h, top hat); one warp per cosmology
+__global__ void k_norm(const CosmoDev* cos, EHConst* eh, TablesDev* tab, int n) {
+  int ci = blockIdx.x;
+  if (ci >= n) return;
+  CosmoDev c = cos[ci];
+  EHConst e = eh[ci];  // built with norm = 1
+  double s = warp_sigmam(c, e, tab[ci].pk, 8., 0);
+  if (threadIdx.x == 0) {
+    double norm = c.sigma8 / s;
+    tab[ci].norm = norm;
+    tab[ci].dz = c.zmax / NZ;
+    eh[ci].ehc = e.ehc * norm * norm;
+  }
+}
+
+// f_K on bin centres and lensing efficiency g (bispectrum.cu:158-190)
+__global__ void k_fk_g(const CosmoDev* cos, const double* nz, int nz_stride, TablesDev* tab, int n) {
+  int ci = blockIdx.x;
+  if (ci >= n) return;
+  const CosmoDev c = cos[ci];
+  TablesDev& t = tab[ci];
+  const double dz = c.zmax / NZ;
+  __shared__ double fk[NZ];
+  for (int i = threadIdx.x; i < NZ; i += blockDim.x) {
+    double zb = (i + 0.5) * dz;
+    double cx = zb / 2, dx = zb / 2, q = 0;
+    for (int m = 0; m < 48; m++) q += c_gq_w[m] * (1. / d_E(c, cx - dx * c_gq_a[m]) + 1. / d_E(c, cx + dx * c_gq_a[m]));
+    fk[i] = C_OVER_H0 * (q * dx);
+    t.f_K[i] = fk[i];
+  }
+  __syncthreads();
+  const double* nzc = nz + (size_t)ci * nz_stride;
+  for (int i = threadIdx.x; i < NZ; i += blockDim.x) {
+    double gi = 0;
+    for (int j = i; j < NZ; j++) {
+      double term = nzc[j] * (fk[j] - fk[i]) / fk[j];
+      gi += (j == i || j == NZ - 1) ? term / 2 : term;
+    }
+    t.g[i] = (i == 0) ? 1.0 : gi * dz;
+  }
+}
+
+// linear growth D1 = lgr(z)/lgr(0) on bin centres (bispectrum.cu:207)
+__global__ void k_growth(const CosmoDev* cos, TablesDev* tab, int n) {
+  int ci = blockIdx.x;
+  if (ci >= n) return;
+  const CosmoDev c = cos[ci];
+  __shared__ double lgr0;
+  if (threadIdx.x == NZ) lgr0 = d_lgr(c, 0.);
+  double v = 0;
+  if (threadIdx.x < NZ) v = d_lgr(c, (threadIdx.x + 0.5) * (c.zmax / NZ));
+  __syncthreads();
+  if (threadIdx.x < NZ) tab[ci].D1[threadIdx.x] = v / lgr0;
+}
+
+// r_sigma by bisection on D1 sigma(1/k) = 1, then n_eff and ncur
+// (bispectrum.cu:202-212, 870-903); one warp per (cosmology, bin)
+__global__ void k_rsigma(const CosmoDev* cos, const EHConst* eh, TablesDev* tab, int n) {
+  int wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  int ci = wid / NZ, bin = wid % NZ;
+  if (ci >= n) return;
+  const CosmoDev c = cos[ci];
+  const EHConst e = eh[ci];
+  TablesDev& t = tab[ci];
+  const double* pk = t.pk;
+  double D1 = t.D1[bin];
+  double rs = 0;
+  if (c.sigma8 >= 1e-8) {
+    double k, k1 = 1., k2 = 1.;
+    bool bad = !isfinite(D1);
+    for (int it = 0; it < 100 && !bad; ++it) {
+      double s = D1 * warp_sigmam(c, e, pk, 1. / k1, 1);
+      if (!isfinite(s)) bad = true;
+      if (s < 1. || bad) break;
+      k1 *= 0.5;
+    }
+    for (int it = 0; it < 100 && !bad; ++it) {
+      double s = D1 * warp_sigmam(c, e, pk, 1. / k2, 1);
+      if (!isfinite(s)) bad = true;
+      if (s > 1. || bad) break;
+      k2 *= 2.;
+    }
+    k = 0.5 * (k1 + k2);
+    for (int it = 0; it < 200 && !bad; ++it) {
+      k = 0.5 * (k1 + k2);
+      double s = D1 * warp_sigmam(c, e, pk, 1. / k, 1);
+      if (!isfinite(s)) {
+        bad = true;
+        break;
+      }
+      if (s < 1.)
+        k1 = k;
+      else if (s > 1.)
+        k2 = k;
+      if (s == 1. || fabs(k2 / k1 - 1.) < EPS * 0.1) break;
+    }
+    rs = bad ? NAN : 1. / k;
+  }
+  double s2 = isfinite(rs) ? warp_sigmam(c, e, pk, rs, 2) : NAN;
+  double s3 = isfinite(rs) ? warp_sigmam(c, e, pk, rs, 3) : NAN;
+  if ((threadIdx.x & 31) == 0) {
+    double d1 = -2. * (D1 * s2) * (D1 * s2);
+    t.r_sigma[bin] = rs;
+    t.n_eff[bin] = -3. + 2. * (D1 * s2) * (D1 * s2);
+    t.ncur[bin] = d1 * d1 + 4. * s3 * D1 * D1;
+  }
+}
+
+// mid-bin two-point interpolation of a z table (bispectrum.cu:335-437) with
+// the lower neighbour clamped at bin 0
+__device__ inline double interp_mid(const double* arr, double zfrac_bins) {
+  int idx = (int)zfrac_bins;
+  double didx = zfrac_bins - idx;
+  if (idx > NZ - 1) {
+    idx = NZ - 1;
+    didx = 1.0;
+  }
+  int ii = idx;
+  double w = 1 - fabs(didx - 0.5), iw = 1 - w;
+  if (didx > 0.5) {
+    if (idx == NZ - 1)
+      iw = 0.0;
+    else
+      ii = idx + 1;
+  } else if (didx < 0.5) {
+    ii = idx - 1 < 0 ? 0 : idx - 1;
+  }
+  return arr[idx] * w + arr[ii] * iw;
+}
+
+// Per-node coefficients of b_kappa's LOS integral (z-only parts of
+// integrand_bkappa + bispec, bispectrum.cu:221-333) and of P_kappa's
+// (limber_integrand_power_spectrum + P_k_nonlinear, bispectrum.cu:531-600,951-991).
+__global__ void k_node_coefs(const CosmoDev* cos, const TablesDev* tab, double* ncoef, float* ncoef_f, double* hcoef,
+                             int n) {
+  int ci = blockIdx.x;
+  int j = threadIdx.x;
+  if (ci >= n || j >= NNODE) return;
+  const CosmoDev c = cos[ci];
+  const TablesDev& t = tab[ci];
+  int i = j >> 1;
+  double cx = c.zmax / 2, dx = c.zmax / 2;
+  double z = (j & 1) ? cx + dx * c_gq_a[i] : cx - dx * c_gq_a[i];
+  double wq = c_gq_w[i] * dx;
+
+  // ---- b_kappa nodes: interpolation index z/zmax*256 (bispectrum.cu:320)
+  {
+    double fb = z / c.zmax * NZ;
+    double g = interp_mid(t.g, fb), fK = interp_mid(t.f_K, fb);
+    double D1 = interp_mid(t.D1, fb), rs = interp_mid(t.r_sigma, fb), ne = interp_mid(t.n_eff, fb);
+    double E = d_E(c, z);
+    double pref = 27. / 8. * c.om * c.om * c.om * pow(H0_OVER_C, 5.0);
+    double gz = g * (1. + z);
+    double W = (z < 1.0e-7) ? 0.0 : wq * pref * gz * gz * gz / fK / E;
+    double ls = log10(D1 * c.sigma8);
+    double a = 1. / (1. + z);
+    double omz = c.om / (c.om + c.ow * pow(a, -3. * c.w));
+    double v[NC_COUNT];
+    v[NC_W] = W;
+    v[NC_S] = rs / fK;
+    v[NC_L2S] = log2(rs / fK);
+    v[NC_HF] = c.h / fK;
+    v[NC_L2HF] = log2(c.h / fK);
+    v[NC_ANA] = LOG2_10 * (-2.167 - 2.944 * ls - 1.106 * ls * ls - 2.865 * ls * ls * ls);
+    v[NC_ANR] = 0.310 * LOG2_10;
+    v[NC_ANC] = pow(10., 0.182 + 0.57 * ne);
+    v[NC_BN] = pow(10., -3.428 - 2.681 * ls + 1.624 * ls * ls - 0.095 * ls * ls * ls);
+    v[NC_CN] = pow(10., 0.159 - 1.107 * ne);
+    v[NC_ALA] = LOG2_10 * (-4.348 - 3.006 * ne - 0.5745 * ne * ne);
+    v[NC_ALD] = LOG2_10 * pow(10., -0.9 + 0.2 * ne);
+    v[NC_BETAB] = pow(10., -1.731 - 2.845 * ne - 1.4995 * ne * ne - 0.2811 * ne * ne * ne);
+    v[NC_FN] = pow(10., -10.533 - 16.838 * ne - 9.3048 * ne * ne - 1.8263 * ne * ne * ne);
+    v[NC_GN] = pow(10., 2.787 + 2.405 * ne + 0.4577 * ne * ne);
+    v[NC_HN] = pow(10., -1.118 - 0.394 * ne);
+    v[NC_MN] = pow(10., -2.605 - 2.434 * ls + 5.71 * ls * ls);
+    v[NC_NN] = pow(10., -4.468 - 3.08 * ls + 1.035 * ls * ls);
+    v[NC_MUN] = pow(10., 15.312 + 22.977 * ne + 10.9579 * ne * ne + 1.6586 * ne * ne * ne);
+    v[NC_NUN] = pow(10., 1.347 + 1.246 * ne + 0.4525 * ne * ne);
+    v[NC_PN] = pow(10., 0.071 - 0.433 * ne);
+    v[NC_EN] = pow(10., -0.632 + 0.646 * ne);
+    v[NC_DN] = pow(10., -0.483 + 0.892 * ls - 0.086 * omz);
+    v[NC_D1SQ] = D1 * D1;
+    v[NC_TREE] = z > 10. ? 1.0 : 0.0;
+    v[NC_D1P4] = D1 * D1 * D1 * D1;
+    double* o = ncoef + (size_t)ci * NC_COUNT * NNODE;
+    float* of = ncoef_f + (size_t)ci * NC_COUNT * NNODE;
+    for (int q = 0; q < NC_COUNT; ++q) {
+      o[q * NNODE + j] = v[q];
+      of[q * NNODE + j] = (float)v[q];
+    }
+  }
+  // ---- P_kappa nodes: interpolation index z/zmax*255 (bispectrum.cu:535,956)
+  {
+    double fb = z / c.zmax * (NZ - 1);
+    double g = interp_mid(t.g, fb), fK = interp_mid(t.f_K, fb);
+    double D1 = interp_mid(t.D1, fb), rs = interp_mid(t.r_sigma, fb);
+    double ne = interp_mid(t.n_eff, fb), ncur = interp_mid(t.ncur, fb);
+    double E = d_E(c, z);
+    double W = (z < 1e-5) ? 0.0
+                          : wq * 9. / 4. * H0_OVER_C * H0_OVER_C * H0_OVER_C * c.om * c.om * (1. + z) * (1. + z) *
+                                g * g / E;
+    double aa = 1. / (1 + z);
+    double den = c.om + aa * (aa * aa * c.ow + (1. - c.om - c.ow));
+    double om_m = c.om / den, om_v = c.ow * aa * aa * aa / den;
+    double nsqr = ne * ne, w = c.w;
+    double f1a = pow(om_m, -0.0732), f2a = pow(om_m, -0.1423), f3a = pow(om_m, 0.0725);
+    double f1b = pow(om_m, -0.0307), f2b = pow(om_m, -0.0585), f3b = pow(om_m, 0.0743);
+    double frac = om_v / (1. - om_m);
+    double v[HC_COUNT];
+    v[HC_W] = W;
+    v[HC_INVFK] = 1.0 / fK;
+    v[HC_RS] = rs;
+    v[HC_D1SQ] = D1 * D1;
+    v[HC_A] = pow(10.0, 1.5222 + 2.8553 * ne + 2.3706 * nsqr + 0.9903 * ne * nsqr + 0.2250 * nsqr * nsqr -
+                            0.6038 * ncur + 0.1749 * om_v * (1.0 + w));
+    v[HC_B] = pow(10.0, -0.5642 + 0.5864 * ne + 0.5716 * nsqr - 1.5474 * ncur + 0.2279 * om_v * (1.0 + w));
+    v[HC_C] = pow(10.0, 0.3698 + 2.0404 * ne + 0.8161 * nsqr + 0.5869 * ncur);
+    v[HC_GAM] = 0.1971 - 0.0843 * ne + 0.8460 * ncur;
+    v[HC_ALPHA] = fabs(6.0835 + 1.3373 * ne - 0.1959 * nsqr - 5.5274 * ncur);
+    v[HC_BETA] = 2.0379 - 0.7354 * ne + 0.3157 * nsqr + 1.2490 * ne * nsqr + 0.3980 * nsqr * nsqr - 0.1682 * ncur;
+    v[HC_XNU] = pow(10.0, 5.2105 + 3.6902 * ne);
+    v[HC_F1] = frac * f1b + (1 - frac) * f1a;
+    v[HC_F2] = frac * f2b + (1 - frac) * f2a;
+    v[HC_F3] = frac * f3b + (1 - frac) * f3a;
+    double* o = hcoef + (size_t)ci * HC_COUNT * NNODE;
+    for (int q = 0; q < HC_COUNT; ++q) o[q * NNODE + j] = v[q];
+  }
+}
+
+// Normalise the LOS weights of the FP32 node table by their maximum (kept in
+// wscale) so that FP32 products stay far from the float range limits, and
+// build the integrand constant blocks.
+__global__ void k_finish(const CosmoDev* cos, const EHConst* eh, const TablesDev* tab, double* ncoef, float* ncoef_f,
+                         double* wscale64, double* wscale32, CosmoK<double>* ck64, CosmoK<float>* ck32, int n) {
+  int ci = blockIdx.x;
+  if (ci >= n) return;
+  __shared__ double wmax;
+  if (threadIdx.x == 0) {
+    double m = 0;
+    const double* W = ncoef + (size_t)ci * NC_COUNT * NNODE + NC_W * NNODE;
+    for (int j = 0; j < NNODE; ++j) m = fmax(m, fabs(W[j]));
+    wmax = m > 0 ? m : 1.0;
+    wscale64[ci] = 1.0;
+    wscale32[ci] = wmax;
+    ck64[ci] = make_cosmok<double>(eh[ci], cos[ci], tab[ci].pk);
+    ck32[ci] = make_cosmok<float>(eh[ci], cos[ci], tab[ci].pk);
+  }
+  __syncthreads();
+  for (int j = threadIdx.x; j < NNODE; j += blockDim.x) {
+    size_t o = (size_t)ci * NC_COUNT * NNODE + NC_W * NNODE + j;
+    ncoef_f[o] = (float)(ncoef[o] / wmax);
+  }
+}
+
+// ---------------------------------------------------------------------------
+void upload_gauss_nodes() {
+  double a[48], w[48];
+  gauss_legendre96(a, w);
+  cudaMemcpyToSymbol(c_gq_a, a, sizeof(a));
+  cudaMemcpyToSymbol(c_gq_w, w, sizeof(w));
+}
+
+cudaError_t build_tables(const CosmoDev* d_cos, EHConst* d_eh, const double* d_nz, int nz_stride, TablesDev* d_tab,
+                         double* d_ncoef, float* d_ncoef_f, double* d_hcoef, double* d_wscale64, double* d_wscale32,
+                         CosmoK<double>* d_ck64, CosmoK<float>* d_ck32, int n, cudaStream_t s) {
+  k_norm<<<n, 32, 0, s>>>(d_cos, d_eh, d_tab, n);
+  k_fk_g<<<n, 256, 0, s>>>(d_cos, d_nz, nz_stride, d_tab, n);
+  k_growth<<<n, NZ + 32, 0, s>>>(d_cos, d_tab, n);
+  long warps = (long)n * NZ;
+  int wpb = 4;
+  k_rsigma<<<(unsigned)((warps + wpb - 1) / wpb), 32 * wpb, 0, s>>>(d_cos, d_eh, d_tab, n);
+  k_node_coefs<<<n, NNODE, 0, s>>>(d_cos, d_tab, d_ncoef, d_ncoef_f, d_hcoef, n);
+  k_finish<<<n, NNODE, 0, s>>>(d_cos, d_eh, d_tab, d_ncoef, d_ncoef_f, d_wscale64, d_wscale32, d_ck64, d_ck32, n);
+  return cudaGetLastError();
+}
+
+}  // namespace tp

@@ -1,0 +1,18 @@
+#pragma once
+#include "tp_bispec.cuh"
+#include "tp_internal.cuh"
+
+namespace tp {
+
+// Uploads the Gauss-Legendre abscissae/weights of the 96-node line-of-sight
+// rules (constant memory of tp_tables.cu) to the current device.
+void upload_gauss_nodes();
+
+// Launches the table build for n cosmologies on stream s: norm, f_K, g, D1,
+// r_sigma, n_eff, ncur, then the per-node coefficient blocks. d_eh must hold
+// make_eh_const(c, 1.0) on entry; its ehc is rescaled by norm^2 on exit.
+cudaError_t build_tables(const CosmoDev* d_cos, EHConst* d_eh, const double* d_nz, int nz_stride, TablesDev* d_tab,
+                         double* d_ncoef, float* d_ncoef_f, double* d_hcoef, double* d_wscale64, double* d_wscale32,
+                         CosmoK<double>* d_ck64, CosmoK<float>* d_ck32, int n, cudaStream_t s);
+
+}  // namespace tp
