@@ -146,6 +146,7 @@ def run_ours(args):
 
         dist.init_process_group("nccl")
     ctx = tp.Context(local)
+    ctx.set_limits(args.region_cap)
     stream = torch.cuda.ExternalStream(ctx.stream_handle, device=local)
     cosmos_all = lhs_cosmologies()
     zs, ns = nz_config()
@@ -200,6 +201,9 @@ def run_ours(args):
         one_step(args.warmup + s, timings)
         torch.cuda.synchronize()
         live_total += int(nlive.sum().item())
+        if args.dump_costs and s == 0:
+            np.savez(args.dump_costs, theta=np.tile(th, (C, 1)), neval=nev.cpu().numpy(), nlive=nlive.cpu().numpy(),
+                     value=out.cpu().numpy())
         bad = int((status != 0).sum().item())
         if bad:
             print(f"warning: {bad} integrals hit a cap in step {s}", file=sys.stderr)
@@ -350,6 +354,8 @@ def main():
     ap.add_argument("--lmax", default="ref")
     ap.add_argument("--cpu-sample", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--region-cap", type=int, default=32768)
+    ap.add_argument("--dump-costs", default="")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
     res = run_reference(args) if args.impl == "reference" else run_ours(args)

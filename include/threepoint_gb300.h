@@ -88,6 +88,12 @@ int tp_ctx_destroy(tp_ctx* ctx);
  * work or CUDA events with the library's asynchronous entry points */
 void* tp_ctx_stream(tp_ctx* ctx);
 
+/* Limits of the adaptive integrals run on this context: region_cap = regions
+ * per integral (default 32768; an integral that needs more stops with
+ * TP_ERR_CAPACITY), max_ctas = CTAs of the persistent grid (0 = all resident).
+ * Device scratch = grid * region_cap * ~90 bytes (3-D integrands). */
+int tp_ctx_set_limits(tp_ctx* ctx, int region_cap, int max_ctas);
+
 /* Measured throughput of the pipes that bound the integrand kernels, whole
  * device: out[0] ex2.approx.f32 (SFU) ops/s, out[1] FP32 FMA/s, out[2] FP64 FMA/s. */
 int tp_pipe_peaks(int device, double* out);

@@ -83,11 +83,25 @@ def test_map3_fp64_matches_oracle(gpu_ctx, oracle_tables):
 
 
 def test_map3_fp32_against_fp64(gpu_ctx):
-    th = [[a * ARC, b * ARC, c * ARC] for a, b, c in ((2, 4, 8), (16, 16, 16), (4, 4, 16))]
+    # includes strongly unequal triplets whose first-rule values are far below
+    # the float range but non-zero in FP64
+    trip = ((2, 4, 8), (16, 16, 16), (4, 4, 16), (1.4697, 3.1748, 21.772), (2.1544, 14.812, 32.0))
+    th = [[a * ARC, b * ARC, c * ARC] for a, b, c in trip]
     v64 = gpu_ctx.map3_batch(th, precision=0)
     v32 = gpu_ctx.map3_batch(th, precision=1)
+    assert np.all(v64 != 0)
     rel = np.abs(v32 - v64) / np.abs(v64)
     assert rel.max() < 1e-3, rel
+
+
+def test_map3_zero_for_disjoint_filters(gpu_ctx, oracle_tables):
+    # (1', 1.47', 32'): all 33 points of the first rule have a zero filter
+    # product in FP64, so the reference's cubature stops at 0 after one region
+    th = [1.0 * ARC, 1.4697 * ARC, 32.0 * ARC]
+    assert oracle_tables.map3(th)[0] == 0.0
+    for prec in (0, 1):
+        v, info = gpu_ctx.map3_batch([th], precision=prec, return_info=True)
+        assert v[0, 0] == 0.0 and info["neval"][0, 0] == 33
 
 
 def test_map3_batch_over_cosmologies(nz256):

@@ -97,6 +97,7 @@ def lib():
         L.tp_pell_batch.argtypes = [p, i, dp, l, i, dp]
         L.tp_map3_batch.argtypes = [p, ip, i, dp, i, d, d, d, d, d, i, dp, dp, i64p, ip]
         L.tp_map3_jobs_device.argtypes = [p, p, p, i, d, d, d, d, d, i, p, p, p, p, p]
+        L.tp_ctx_set_limits.argtypes = [p, i, i]
         L.tp_ctx_stream.restype = p
         L.tp_ctx_stream.argtypes = [p]
         L.tp_pipe_peaks.argtypes = [i, dp]
@@ -175,6 +176,10 @@ class Context:
         _check(None, lib().tp_ctx_create(device, C.byref(self._h)))
         self.n_cosmo = 0
         self.cosmologies = []
+
+    def set_limits(self, region_cap=32768, max_ctas=0):
+        """Regions per adaptive integral and CTAs of the persistent grid."""
+        _check(self._h, lib().tp_ctx_set_limits(self._h, region_cap, max_ctas))
 
     def close(self):
         if self._h:

@@ -133,6 +133,39 @@ __device__ inline void make_tri(double l1, double l2, double l3, Tri<R>& T) {
   T.f2t[2] = (R)f2_tree(l3, l1, l2);
 }
 
+// FP32 triangle setup from (l1, l2, phi) of the <Map^3> parametrisation
+// (l3^2 = l1^2 + l2^2 + 2 l1 l2 cos phi), written without cancellation:
+// l3^2 = (l1-l2)^2 + 4 l1 l2 cos^2(phi/2), and the three F2_tree cosines from
+// the closed triangle l1 + l2 + l3 = 0: cos12 = cos phi,
+// cos23 = -(l1 cos phi + l2)/l3, cos31 = -(l1 + l2 cos phi)/l3.
+__device__ __forceinline__ float f2t_cos(float c, float a, float b) {
+  return (5.f / 7.f) + 0.5f * c * (a / b + b / a) + (2.f / 7.f) * c * c;
+}
+__device__ __forceinline__ void make_tri_phi_f(float l1, float l2, float cphi, float l3, Tri<float>& T) {
+  typedef Mth<float> M;
+  T.l[0] = l1;
+  T.l[1] = l2;
+  T.l[2] = l3;
+  T.lg[0] = M::lg2(l1);
+  T.lg[1] = M::lg2(l2);
+  T.lg[2] = M::lg2(l3);
+  float a = l1, b = l2, c = l3, la = T.lg[0], lb = T.lg[1], lc = T.lg[2], t;
+  if (a < b) { t = a; a = b; b = t; t = la; la = lb; lb = t; }
+  if (a < c) { t = a; a = c; c = t; t = la; la = lc; lc = t; }
+  if (b < c) { t = b; b = c; c = t; t = lb; lb = lc; lc = t; }
+  float ia = M::rcp(a);
+  float r2 = (b + c - a) * ia;
+  T.log2r1 = lc - la;
+  T.r2sq = r2 * r2;
+  T.pr2 = M::ex2((float)(LOG2_10 * 0.007) * r2);
+  float il3 = M::rcp(l3);
+  float c23 = -(l1 * cphi + l2) * il3;
+  float c31 = -(l1 + l2 * cphi) * il3;
+  T.f2t[0] = f2t_cos(cphi, l1, l2);
+  T.f2t[1] = f2t_cos(c23, l2, l3);
+  T.f2t[2] = f2t_cos(c31, l3, l1);
+}
+
 // B(ell_i / f_K(z_j), z_j) for node j; nc points at the node table of the
 // cosmology (coef c of node j at nc[c*NNODE + j]).
 template <typename R>

@@ -440,8 +440,14 @@ extern "C" int tp_bkappa_batch(tp_ctx* ctx, const int* cosmo_index, const double
 // ---------------------------------------------------------------------------
 // <Map^3>
 // ---------------------------------------------------------------------------
-static const int MAP3_CAP = 1 << 16;
 static const int MAP3_MAX_SWEEPS = 2000;
+
+extern "C" int tp_ctx_set_limits(tp_ctx* ctx, int region_cap, int max_ctas) {
+  if (!ctx || region_cap < 64 || max_ctas < 0) return TP_ERR_ARG;
+  ctx->region_cap = region_cap;
+  ctx->max_ctas = max_ctas;
+  return TP_OK;
+}
 
 extern "C" int tp_map3_jobs_device(tp_ctx* ctx, const int* job_cosmo, const double* job_theta, int n_jobs,
                                    double phi_min, double phi_max, double l_min, double l_max, double rel_tol,
@@ -455,7 +461,7 @@ extern "C" int tp_map3_jobs_device(tp_ctx* ctx, const int* job_cosmo, const doub
   cudaSetDevice(ctx->device);
   int grid = 0;
   size_t smem = 0, scratch = 0;
-  cudaError_t e = plan_map3(precision, n_jobs, MAP3_CAP, ctx->max_ctas, &grid, &smem, &scratch);
+  cudaError_t e = plan_map3(precision, n_jobs, ctx->region_cap, ctx->max_ctas, &grid, &smem, &scratch);
   if (e != cudaSuccess) return tp_cuda(ctx, e, "map3 plan");
   int st = ctx->ensure_scratch(scratch);
   if (st) return st;
@@ -475,7 +481,7 @@ extern "C" int tp_map3_jobs_device(tp_ctx* ctx, const int* job_cosmo, const doub
   L.phimin = phi_min;
   L.phimax = phi_max;
   L.rel_tol = rel_tol;
-  L.cap = MAP3_CAP;
+  L.cap = ctx->region_cap;
   L.max_sweeps = MAP3_MAX_SWEEPS;
   L.out = out;
   L.err = err;

@@ -11,7 +11,8 @@ struct tp_ctx {
   int device = 0;
   cudaStream_t stream = nullptr;
   std::string err;
-  int max_ctas = 0;  // 0 = all resident CTAs
+  int max_ctas = 0;        // 0 = all resident CTAs
+  int region_cap = 32768;  // regions per adaptive integral
 
   // cosmologies and their device tables
   int n_cosmo = 0;

@@ -307,6 +307,8 @@ __device__ inline bool converged_check(int fdim, int norm, const double* V, cons
 // Shared scratch of the engine (besides the policy's own)
 template <int FDIM>
 struct EngineShared {
+  int live_list[1024];  // live points of the current chunk
+  int nlive_chunk;
   double hist[256];
   double red[64];
   int ired[80];
@@ -321,8 +323,9 @@ struct EngineShared {
 // The persistent adaptive-integration kernel body. Policy P provides:
 //   static constexpr int G, REC (bytes per point record), CH (regions/chunk)
 //   __device__ void begin_job(int job, char* psmem, double* xmin, double* xmax) (all threads; syncs inside)
-//   __device__ void setup(int p, const double* x, char* rec)
-//   __device__ void group(const char* rec, int g, double* part /*FDIM*/)
+//   __device__ bool setup(int p, const double* x, char* rec)   (true: point needs its groups)
+//   __device__ bool is_live(const char* rec)
+//   __device__ void group(const char* rec, int g, double* part /*FDIM*/)  (live points only)
 //   __device__ void finalize(const char* rec, const double* sum /*FDIM*/, double* fval /*FDIM*/)
 //   __device__ void end_job(int job, const double* V, const double* E, long long neval, int status)
 //   static constexpr size_t PSMEM (policy shared bytes)
@@ -332,6 +335,7 @@ __device__ void adaptive_body(P& pol, int njobs, int* job_counter, const EngineC
   constexpr int NP = GMRule<DIM>::NP;
   constexpr int CH = P::CH;
   constexpr int G = P::G;
+  static_assert(P::CH * NP <= 1024, "live list holds one chunk");
   extern __shared__ __align__(16) char smem[];
   char* psmem = smem;
   char* recs = psmem + ((P::PSMEM + 15) & ~size_t(15));
@@ -365,6 +369,7 @@ __device__ void adaptive_body(P& pol, int njobs, int* job_counter, const EngineC
       es->stop = 0;
       es->neval = 0;
       es->sweeps = 0;
+      es->nlive_chunk = 0;
     }
     __syncthreads();
 
@@ -374,6 +379,8 @@ __device__ void adaptive_body(P& pol, int njobs, int* job_counter, const EngineC
       for (int base = 0; base < npend; base += CH) {
         const int nreg = min(CH, npend - base);
         const int npts = nreg * NP;
+        // (a) point setup; points that need the expensive inner sums are
+        //     appended to a compact live list
         for (int p = tid; p < npts; p += NT) {
           int r = S.pend[base + p / NP];
           double c[DIM], h[DIM], x[DIM];
@@ -383,26 +390,32 @@ __device__ void adaptive_body(P& pol, int njobs, int* job_counter, const EngineC
             h[d] = S.hw[(size_t)d * S.cap + r];
           }
           rule_point<DIM>(p % NP, c, h, x);
-          pol.setup(p, x, recs + (size_t)p * P::REC);
+          if (pol.setup(p, x, recs + (size_t)p * P::REC)) es->live_list[atomicAdd(&es->nlive_chunk, 1)] = p;
         }
         __syncthreads();
-        for (int it = tid; it < npts * G; it += NT) {
-          int g = it / npts, p = it - g * npts;
+        // (b) (live point, group) items: equal-cost work for every thread
+        const int nl = es->nlive_chunk;
+        for (int it = tid; it < nl * G; it += NT) {
+          int g = it / nl, q = it - g * nl;
+          int p = es->live_list[q];
           double pv[FDIM];
           pol.group(recs + (size_t)p * P::REC, g, pv);
 #pragma unroll
           for (int k = 0; k < FDIM; ++k) part[((size_t)g * npts + p) * FDIM + k] = pv[k];
         }
         __syncthreads();
+        // (c) per-point totals (fixed group order -> deterministic)
         for (int p = tid; p < npts; p += NT) {
           double s[FDIM];
 #pragma unroll
           for (int k = 0; k < FDIM; ++k) s[k] = 0;
-          for (int g = 0; g < G; ++g)
+          if (pol.is_live(recs + (size_t)p * P::REC))
+            for (int g = 0; g < G; ++g)
 #pragma unroll
-            for (int k = 0; k < FDIM; ++k) s[k] += part[((size_t)g * npts + p) * FDIM + k];
+              for (int k = 0; k < FDIM; ++k) s[k] += part[((size_t)g * npts + p) * FDIM + k];
           pol.finalize(recs + (size_t)p * P::REC, s, fval + (size_t)p * FDIM);
         }
+        if (tid == 0) es->nlive_chunk = 0;
         __syncthreads();
         for (int rr = tid; rr < nreg; rr += NT) {
           int r = S.pend[base + rr];
