@@ -989,7 +989,8 @@ extern "C" void orc_gq96(double* a, double* w) {
 }
 extern "C" void orc_set_threads(int n) {
 #ifdef _OPENMP
-  if (n > 0) omp_set_num_threads(n);
+  if (n <= 0) n = omp_get_num_procs();
+  omp_set_num_threads(n);
 #else
   (void)n;
 #endif

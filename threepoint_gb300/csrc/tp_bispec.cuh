@@ -166,32 +166,32 @@ __device__ __forceinline__ void make_tri_phi_f(float l1, float l2, float cphi, f
   T.f2t[2] = f2t_cos(c31, l3, l1);
 }
 
-// B(ell_i / f_K(z_j), z_j) for node j; nc points at the node table of the
-// cosmology (coef c of node j at nc[c*NNODE + j]).
+// B at one redshift from its coefficient vector nc[c * stride] (c = NC_*),
+// for a triangle whose ell_i = T.l[i] * sc (log2: T.lg[i] + l2sc):
+// q_i = ell_i * s, k_i h = ell_i * hf.
 template <typename R>
-__device__ __forceinline__ R bispec_node(const R* __restrict__ nc, int j, const Tri<R>& T, const CosmoK<R>& K) {
+__device__ __forceinline__ R bispec_eval(const R* __restrict__ nc, int stride, R s, R l2s, R hf, R l2hf,
+                                         const Tri<R>& T, const CosmoK<R>& K) {
   typedef Mth<R> M;
-  const R s = nc[NC_S * NNODE + j], l2s = nc[NC_L2S * NNODE + j];
-  const R hf = nc[NC_HF * NNODE + j], l2hf = nc[NC_L2HF * NNODE + j];
+#define NCV(c) nc[(c) * stride]
   R q[3], lq[3], P[3];
 #pragma unroll
   for (int i = 0; i < 3; ++i) {
     q[i] = T.l[i] * s;
     lq[i] = T.lg[i] + l2s;
   }
-  if (nc[NC_TREE * NNODE + j] != (R)0) {
+  if (NCV(NC_TREE) != (R)0) {
     // tree level for z > 10 (bispectrum.cu:229-230,695-698)
 #pragma unroll
     for (int i = 0; i < 3; ++i) P[i] = plin<R>(K, T.l[i] * hf, T.lg[i] + l2hf);
-    return nc[NC_D1P4 * NNODE + j] * (R)2 *
-           (T.f2t[0] * P[0] * P[1] + T.f2t[1] * P[1] * P[2] + T.f2t[2] * P[2] * P[0]);
+    return NCV(NC_D1P4) * (R)2 * (T.f2t[0] * P[0] * P[1] + T.f2t[1] * P[1] * P[2] + T.f2t[2] * P[2] * P[0]);
   }
   // 1-halo term (B4, B7)
-  const R an = M::ex2(nc[NC_ANA * NNODE + j] - nc[NC_ANR * NNODE + j] * M::ex2(nc[NC_ANC * NNODE + j] * T.log2r1));
-  R al = M::ex2(nc[NC_ALA * NNODE + j] + nc[NC_ALD * NNODE + j] * T.r2sq);
+  const R an = M::ex2(NCV(NC_ANA) - NCV(NC_ANR) * M::ex2(NCV(NC_ANC) * T.log2r1));
+  R al = M::ex2(NCV(NC_ALA) + NCV(NC_ALD) * T.r2sq);
   al = al > K.alpha_max ? K.alpha_max : al;
-  const R be = nc[NC_BETAB * NNODE + j] * T.pr2;
-  const R bn = nc[NC_BN * NNODE + j], cn = nc[NC_CN * NNODE + j];
+  const R be = NCV(NC_BETAB) * T.pr2;
+  const R bn = NCV(NC_BN), cn = NCV(NC_CN);
   R bs1h = (R)1;
 #pragma unroll
   for (int i = 0; i < 3; ++i) {
@@ -199,11 +199,11 @@ __device__ __forceinline__ R bispec_node(const R* __restrict__ nc, int j, const 
     bs1h *= cq * M::rcp((an * M::ex2(al * lq[i]) + bn * M::ex2(be * lq[i])) * (cq + (R)1));
   }
   // 3-halo term (B5, B6, B9)
-  const R fn = nc[NC_FN * NNODE + j], gn = nc[NC_GN * NNODE + j], hn = nc[NC_HN * NNODE + j];
-  const R mn = nc[NC_MN * NNODE + j], nn = nc[NC_NN * NNODE + j];
-  const R mun = nc[NC_MUN * NNODE + j], nun = nc[NC_NUN * NNODE + j];
-  const R pn = nc[NC_PN * NNODE + j], en = nc[NC_EN * NNODE + j];
-  const R d1sq = nc[NC_D1SQ * NNODE + j];
+  const R fn = NCV(NC_FN), gn = NCV(NC_GN), hn = NCV(NC_HN);
+  const R mn = NCV(NC_MN), nn = NCV(NC_NN);
+  const R mun = NCV(NC_MUN), nun = NCV(NC_NUN);
+  const R pn = NCV(NC_PN), en = NCV(NC_EN);
+  const R d1sq = NCV(NC_D1SQ);
 #pragma unroll
   for (int i = 0; i < 3; ++i) {
     R qi = q[i];
@@ -214,11 +214,101 @@ __device__ __forceinline__ R bispec_node(const R* __restrict__ nc, int j, const 
     R mq = mn * M::ex2(mun * lq[i]) + nn * M::ex2(nun * lq[i]);
     P[i] = a + x3 * M::rcp(mq * (x3 + (R)1));
   }
-  const R dn = nc[NC_DN * NNODE + j];
+  const R dn = NCV(NC_DN);
   R bs3h = (R)2 * ((T.f2t[0] + dn * q[2]) * P[0] * P[1] + (T.f2t[1] + dn * q[0]) * P[1] * P[2] +
                    (T.f2t[2] + dn * q[1]) * P[2] * P[0]);
   bs3h *= M::rcp(((R)1 + en * q[0]) * ((R)1 + en * q[1]) * ((R)1 + en * q[2]));
+#undef NCV
   return bs1h + bs3h;
+}
+
+// B(ell_i / f_K(z_j), z_j) at line-of-sight node j of a node table
+// (coef c of node j at nc[c*NNODE + j]).
+template <typename R>
+__device__ __forceinline__ R bispec_node(const R* __restrict__ nc, int j, const Tri<R>& T, const CosmoK<R>& K) {
+  return bispec_eval<R>(nc + j, NNODE, nc[NC_S * NNODE + j], nc[NC_L2S * NNODE + j], nc[NC_HF * NNODE + j],
+                        nc[NC_L2HF * NNODE + j], T, K);
+}
+
+// Mid-bin two-point interpolation of a z table at fractional bin position fb
+// (cuda_version/bispectrum.cu:335-437) with the lower neighbour clamped at bin 0.
+__host__ __device__ inline void interp_mid_w(double fb, int& i0, int& i1, double& w0, double& w1) {
+  int idx = (int)fb;
+  double didx = fb - idx;
+  if (idx > NZ - 1) {
+    idx = NZ - 1;
+    didx = 1.0;
+  }
+  int ii = idx;
+  double w = 1 - fabs(didx - 0.5), iw = 1 - w;
+  if (didx > 0.5) {
+    if (idx == NZ - 1)
+      iw = 0.0;
+    else
+      ii = idx + 1;
+  } else if (didx < 0.5) {
+    ii = idx - 1 < 0 ? 0 : idx - 1;
+  }
+  i0 = idx;
+  i1 = ii;
+  w0 = w;
+  w1 = iw;
+}
+
+// BiHalofit coefficients of one arbitrary redshift z (the z-only part of
+// integrand_bkappa + bispec, bispectrum.cu:221-333), into zc[NC_*] with
+// NC_W = (g(1+z))^3 / f_K / E(z) (no quadrature weight). Returns false when
+// integrand_bkappa is zero at this z (z < 1e-7).
+template <typename R>
+__device__ inline bool zcoefs(const TablesDev& t, const CosmoDev& c, double z, R* zc) {
+  if (z < 1.0e-7) return false;
+  int i0, i1;
+  double w0, w1;
+  interp_mid_w(z / c.zmax * NZ, i0, i1, w0, w1);
+  double g = t.g[i0] * w0 + t.g[i1] * w1, fK = t.f_K[i0] * w0 + t.f_K[i1] * w1;
+  double D1 = t.D1[i0] * w0 + t.D1[i1] * w1, rs = t.r_sigma[i0] * w0 + t.r_sigma[i1] * w1;
+  double ned = t.n_eff[i0] * w0 + t.n_eff[i1] * w1;
+  typedef Mth<R> M;
+  const R L10 = (R)LOG2_10;
+  R zp = (R)(1.0 + z);
+  R l2zp = M::lg2(zp);
+  R E = sqrt((R)c.om * zp * zp * zp + (R)c.ow * M::ex2((R)(3 * (1.0 + c.w)) * l2zp));
+  R gz = (R)g * zp;
+  R fKr = (R)fK;
+  zc[NC_W] = gz * gz * gz / fKr / E;
+  R sr = (R)(rs / fK);
+  zc[NC_S] = sr;
+  zc[NC_L2S] = M::lg2(sr);
+  R hf = (R)(c.h / fK);
+  zc[NC_HF] = hf;
+  zc[NC_L2HF] = M::lg2(hf);
+  R ls = M::lg2((R)(D1 * c.sigma8)) * (R)0.30102999566398119521;
+  R ne = (R)ned;
+  R aexp = M::ex2((R)(-3. * c.w) * (-l2zp));  // a^(-3w), a = 1/(1+z)
+  R omz = (R)c.om / ((R)c.om + (R)c.ow * aexp);
+  zc[NC_ANA] = L10 * ((R)-2.167 + ls * ((R)-2.944 + ls * ((R)-1.106 + ls * (R)-2.865)));
+  zc[NC_ANR] = (R)(0.310 * LOG2_10);
+  zc[NC_ANC] = M::ex2(L10 * ((R)0.182 + (R)0.57 * ne));
+  zc[NC_BN] = M::ex2(L10 * ((R)-3.428 + ls * ((R)-2.681 + ls * ((R)1.624 + ls * (R)-0.095))));
+  zc[NC_CN] = M::ex2(L10 * ((R)0.159 - (R)1.107 * ne));
+  zc[NC_ALA] = L10 * ((R)-4.348 + ne * ((R)-3.006 + ne * (R)-0.5745));
+  zc[NC_ALD] = L10 * M::ex2(L10 * ((R)-0.9 + (R)0.2 * ne));
+  zc[NC_BETAB] = M::ex2(L10 * ((R)-1.731 + ne * ((R)-2.845 + ne * ((R)-1.4995 + ne * (R)-0.2811))));
+  zc[NC_FN] = M::ex2(L10 * ((R)-10.533 + ne * ((R)-16.838 + ne * ((R)-9.3048 + ne * (R)-1.8263))));
+  zc[NC_GN] = M::ex2(L10 * ((R)2.787 + ne * ((R)2.405 + ne * (R)0.4577)));
+  zc[NC_HN] = M::ex2(L10 * ((R)-1.118 - (R)0.394 * ne));
+  zc[NC_MN] = M::ex2(L10 * ((R)-2.605 + ls * ((R)-2.434 + ls * (R)5.71)));
+  zc[NC_NN] = M::ex2(L10 * ((R)-4.468 + ls * ((R)-3.08 + ls * (R)1.035)));
+  zc[NC_MUN] = M::ex2(L10 * ((R)15.312 + ne * ((R)22.977 + ne * ((R)10.9579 + ne * (R)1.6586))));
+  zc[NC_NUN] = M::ex2(L10 * ((R)1.347 + ne * ((R)1.246 + ne * (R)0.4525)));
+  zc[NC_PN] = M::ex2(L10 * ((R)0.071 - (R)0.433 * ne));
+  zc[NC_EN] = M::ex2(L10 * ((R)-0.632 + (R)0.646 * ne));
+  zc[NC_DN] = M::ex2(L10 * ((R)-0.483 + (R)0.892 * ls - (R)0.086 * omz));
+  R d1 = (R)D1;
+  zc[NC_D1SQ] = d1 * d1;
+  zc[NC_TREE] = z > 10. ? (R)1 : (R)0;
+  zc[NC_D1P4] = d1 * d1 * d1 * d1;
+  return true;
 }
 
 __device__ __forceinline__ double uhat(double eta) {

@@ -1,0 +1,414 @@
+// Natural components Gamma^0..Gamma^3 of the shear three-point correlation
+// function: 3-D adaptive cubature over (z, phi, psi) of the Ogata Hankel sum
+// of the BiHalofit convergence bispectrum at redshift z.
+//
+// Reference: gamma0..gamma3 (cuda_version/gamma.cu:98-148), the integrands
+// full_integrand_gamma0/1 and one_integrand_gamma0 (:419-482), the triangle
+// geometry interior_angle, A, alpha, betabar, prefactor (:484-529), the Ogata
+// nodes of compute_weights_bessel (:13-68) and the orthocentre-to-centroid
+// rotation (:72-96; CONVERT_TO_CENTROID, gamma.cuh:25).
+//
+// One job = (triangle, component). A point record holds the z-only BiHalofit
+// coefficients of its redshift, the unit triangle shape (cos psi, sin psi,
+// ...) and per cyclic term j the scale A_j and complex weight C_j; a
+// (point, group) item evaluates 4 Ogata nodes x 3 terms = 12 bispectra.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <complex>
+#include <string>
+#include <vector>
+
+#include "tp_bispec.cuh"
+#include "tp_capi_internal.h"
+#include "tp_cubature.cuh"
+#include "tp_internal.cuh"
+#include "tp_kernels.cuh"
+
+namespace tp {
+
+constexpr int PREC_K = 33;       // int(3.31/0.1) Ogata nodes (index 0 unused), gamma.cuh:29-30
+constexpr double PREC_H = 0.1;
+
+struct OgataTab {
+  double psi[2][PREC_K], prod[2][PREC_K], l2psi[2][PREC_K];  // [0]: J6 (Gamma0), [1]: J2 (Gamma1)
+};
+__constant__ OgataTab c_og;
+
+// zeros of J_nu by Newton iteration from McMahon's expansion (s >= 1); s = 0 -> 0
+static double bessel_zero(int nu, int s) {
+  if (s == 0) return 0.0;
+  double mu = 4.0 * nu * nu;
+  double b = (s + 0.5 * nu - 0.25) * PI;
+  double x = b - (mu - 1) / (8 * b) - 4 * (mu - 1) * (7 * mu - 31) / (3 * pow(8 * b, 3));
+  if (s == 1) x = nu + 1.8557571 * cbrt((double)nu) + 1.033150 / cbrt((double)nu);
+  for (int it = 0; it < 100; ++it) {
+    double J = std::cyl_bessel_j((double)nu, x);
+    double dJ = 0.5 * (std::cyl_bessel_j((double)nu - 1, x) - std::cyl_bessel_j((double)nu + 1, x));
+    double dx = J / dJ;
+    x -= dx;
+    if (fabs(dx) < 1e-15 * x) break;
+  }
+  return x;
+}
+
+static void ogata_host(OgataTab& o) {
+  for (int pass = 0; pass < 2; ++pass) {
+    int nu = pass == 0 ? 6 : 2;
+    for (int i = 0; i < PREC_K; ++i) {
+      double zr = bessel_zero(nu, i), pz = zr / PI;
+      double t = pz * PREC_H;
+      double psi = PI * (t * tanh(PI * sinh(t) / 2)) / PREC_H;
+      double psip = (sinh(PI * sinh(t)) + PI * t * cosh(t)) / (cosh(PI * sinh(t)) + 1);
+      double Jn1 = i == 0 ? 0.0 : std::cyl_bessel_j((double)nu + 1, zr);
+      double w = 2 / (PI * zr * Jn1 * Jn1);
+      o.psi[pass][i] = psi;
+      o.prod[pass][i] = i == 0 ? 0.0 : w * psi * psi * psi * std::cyl_bessel_j((double)nu, psi) * psip;
+      o.l2psi[pass][i] = i == 0 ? 0.0 : log2(psi);
+    }
+  }
+}
+
+cudaError_t gamma_upload_constants() {
+  static OgataTab o;
+  static bool built = false;
+  if (!built) {
+    ogata_host(o);
+    built = true;
+  }
+  return cudaMemcpyToSymbol(c_og, &o, sizeof(o));
+}
+
+// geometry (gamma.cu:491-529), double precision
+__host__ __device__ inline double interior_angle(double an1, double an2, double opp) {
+  return acos((an1 * an1 + an2 * an2 - opp * opp) / (2.0 * an1 * an2));
+}
+__host__ __device__ inline double height_of_triangle(double x1, double x2, double x3) {
+  return 0.5 * sqrt(2 * x1 * x1 + 2 * x2 * x2 - x3 * x3);
+}
+__host__ __device__ inline double one_rotation_angle_otc(double x1, double x2, double x3) {
+  double psi3 = interior_angle(x1, x2, x3);
+  double h3 = height_of_triangle(x1, x2, x3);
+  double d = x2 * x2 - x1 * x1;
+  double s = x1 * x2 * sin(psi3);
+  double c2 = (d * d - 4 * s * s) / ((2 * h3 * x3) * (2 * h3 * x3));
+  double s2 = d * x1 * x2 * sin(psi3) / ((h3 * x3) * (h3 * x3));
+  return atan2(s2, c2) / 2;
+}
+
+struct GammaJobs {
+  const double* x;  // [n_tri][3]
+  const int* comp;  // [n_jobs]
+  const int* tri;   // [n_jobs]
+};
+
+template <typename R>
+struct GammaPolicy {
+  static constexpr int G = 8;     // groups of 4 Ogata nodes
+  static constexpr int KPG = 4;
+  static constexpr int CH = 4;    // regions per chunk (records are large)
+  struct Rec {
+    R zc[NC_COUNT];
+    Tri<R> tri;      // unit-scale triangle (cos psi, sin psi, ell3/psi_k)
+    R invA[3], l2A[3];
+    R cre[3], cim[3];
+    R bmin;
+    int live;
+  };
+  static constexpr int REC = (int)sizeof(Rec);
+  static constexpr size_t PSMEM = sizeof(CosmoK<R>) + 64;
+
+  GammaJobs J;
+  const TablesDev* tab;
+  const CosmoDev* cosm;
+  const CosmoK<R>* ck;
+  int cosmo;
+  double* out;  // [n_tri][4][2]
+  int* status;  // [n_tri]
+  // per-job state
+  CosmoK<R>* s_ck;
+  int which;                      // 0: Gamma0 integrand, 1: Gamma1 integrand
+  double x1, x2, x3;              // sides passed to the integrand (permuted for Gamma2/3)
+  double vp[3], ph0[3];           // Gamma0: varpsi_j, constant phase of term j
+  double p1, p2, p3;              // Gamma1: interior angles
+  double zmax;
+
+  __device__ void begin_job(int job, char* psmem, double* xmin, double* xmax) {
+    s_ck = (CosmoK<R>*)psmem;
+    if (threadIdx.x == 0) *s_ck = ck[cosmo];
+    const int t = J.tri[job], c = J.comp[job];
+    double a = J.x[3 * t], b = J.x[3 * t + 1], d = J.x[3 * t + 2];
+    which = c == 0 ? 0 : 1;
+    if (c <= 1) {
+      x1 = a, x2 = b, x3 = d;
+    } else if (c == 2) {
+      x1 = b, x2 = d, x3 = a;  // gamma2 = gamma1(x2, x3, x1)
+    } else {
+      x1 = d, x2 = a, x3 = b;  // gamma3 = gamma1(x3, x1, x2)
+    }
+    const double xs[3][3] = {{x1, x2, x3}, {x2, x3, x1}, {x3, x1, x2}};
+    for (int j = 0; j < 3; ++j) {
+      vp[j] = interior_angle(xs[j][0], xs[j][1], xs[j][2]);
+      ph0[j] = interior_angle(xs[j][1], xs[j][2], xs[j][0]) - interior_angle(xs[j][0], xs[j][2], xs[j][1]);
+    }
+    p1 = interior_angle(x2, x3, x1);
+    p2 = interior_angle(x3, x1, x2);
+    p3 = interior_angle(x1, x2, x3);
+    zmax = cosm[cosmo].zmax;
+    xmin[0] = 0;
+    xmin[1] = 0;
+    xmin[2] = 0;
+    xmax[0] = zmax;
+    xmax[1] = 2 * PI;
+    xmax[2] = PI / 2;
+    __syncthreads();
+  }
+
+  __device__ bool is_live(const char* recp) const { return ((const Rec*)recp)->live != 0; }
+
+  __device__ bool setup(int p, const double* x, char* recp) {
+    (void)p;
+    Rec& r = *(Rec*)recp;
+    const double z = x[0], phi = x[1], psi = x[2];
+    r.live = zcoefs<R>(tab[cosmo], cosm[cosmo], z, r.zc);
+    if (!r.live) return false;
+    // the geometry is evaluated in double: a few dozen operations per point
+    // against 96 bispectra
+    double cp = cos(psi), sp = sin(psi), s2p = sin(2 * psi), c2p = cos(2 * psi);
+    double cph = cos(phi), sph = sin(phi);
+    double bb = 0.5 * atan2(c2p * sph, cph + s2p);  // betabar, gamma.cu:524-529
+    double b3s = cp * cp + sp * sp + 2 * cp * sp * cph;
+    double b3 = b3s <= 0 ? 0.0 : sqrt(b3s);
+    r.bmin = (R)fmin(cp, fmin(sp, b3));
+    if (!(b3 > 0 && cp > 0 && sp > 0)) {
+      r.live = 0;
+      return false;
+    }
+    if constexpr (sizeof(R) == 4)
+      make_tri_phi_f((float)cp, (float)sp, (float)cph, (float)b3, *(Tri<float>*)&r.tri);
+    else
+      make_tri<R>(cp, sp, b3, r.tri);
+    if (which == 0) {
+      const double xs[3][2] = {{x1, x2}, {x2, x3}, {x3, x1}};
+      for (int j = 0; j < 3; ++j) {
+        double a = xs[j][0], b = xs[j][1];
+        double ang = phi + vp[j];
+        double A = sqrt((cp * b) * (cp * b) + (sp * a) * (sp * a) + s2p * a * b * cos(ang));
+        double al = atan2((cp * b - sp * a) * sin(ang / 2), (cp * b + sp * a) * cos(ang / 2));
+        double phase = ph0[j] - 6 * al + 2 * bb;
+        double mag = s2p * PI / (A * A * A * A);
+        r.invA[j] = (R)(1.0 / A);
+        r.l2A[j] = (R)log2(A);
+        r.cre[j] = (R)(mag * cos(phase));
+        r.cim[j] = (R)(mag * sin(phase));
+      }
+    } else {
+      // term order as full_integrand_gamma1: j=0 -> A1, 1 -> A2, 2 -> A3
+      const double ab[3][2] = {{x2, x3}, {x3, x1}, {x1, x2}};
+      const double vps[3] = {p1, p2, p3};
+      double ph[3];
+      double alv[3], Av[3];
+      for (int j = 0; j < 3; ++j) {
+        double a = ab[j][0], b = ab[j][1];
+        double ang = phi + vps[j];
+        Av[j] = sqrt((cp * b) * (cp * b) + (sp * a) * (sp * a) + s2p * a * b * cos(ang));
+        alv[j] = atan2((cp * b - sp * a) * sin(ang / 2), (cp * b + sp * a) * cos(ang / 2));
+      }
+      ph[0] = p3 - p2 - 2 * (bb + alv[0]);
+      ph[1] = p3 - p1 - 2 * p2 + 2 * (bb + phi - alv[1]);
+      ph[2] = p1 - p2 + 2 * p3 + 2 * (bb - phi - alv[2]);
+      for (int j = 0; j < 3; ++j) {
+        double mag = s2p * PI / (Av[j] * Av[j] * Av[j] * Av[j]);
+        r.invA[j] = (R)(1.0 / Av[j]);
+        r.l2A[j] = (R)log2(Av[j]);
+        r.cre[j] = (R)(mag * cos(ph[j]));
+        r.cim[j] = (R)(mag * sin(ph[j]));
+      }
+    }
+    return true;
+  }
+
+  __device__ void group(const char* recp, int g, double* pv) {
+    const Rec& r = *(const Rec*)recp;
+    const CosmoK<R> K = *s_ck;
+    const int og = which;
+    KSum<R> are, aim;
+    const R* zc = r.zc;
+    const R s = zc[NC_S], l2s = zc[NC_L2S], hf = zc[NC_HF], l2hf = zc[NC_L2HF], W = zc[NC_W];
+    for (int kk = 0; kk < KPG; ++kk) {
+      const int k = 1 + g * KPG + kk;
+      const R psik = (R)c_og.psi[og][k], l2psik = (R)c_og.l2psi[og][k], prodk = (R)c_og.prod[og][k];
+#pragma unroll
+      for (int j = 0; j < 3; ++j) {
+        R sc = psik * r.invA[j];
+        if (r.bmin * sc <= (R)1.0e-10) continue;  // integrand_bkappa: ell <= 1e-10 -> 0
+        R l2sc = l2psik - r.l2A[j];
+        R B = bispec_eval<R>(zc, 1, s * sc, l2s + l2sc, hf * sc, l2hf + l2sc, r.tri, K);
+        R v = W * B;
+        if (v != v) v = (R)0;  // NaN -> 0 (bispectrum.cu:327-331)
+        v *= prodk;
+        are.add(r.cre[j] * v);
+        aim.add(r.cim[j] * v);
+      }
+    }
+    pv[0] = (double)are.s;
+    pv[1] = (double)aim.s;
+  }
+
+  __device__ void finalize(const char* recp, const double* sum, double* fv) {
+    const Rec& r = *(const Rec*)recp;
+    fv[0] = r.live ? sum[0] : 0.0;
+    fv[1] = r.live ? sum[1] : 0.0;
+  }
+
+  __device__ void end_job(int job, const double* V, const double* E, long long nev, int st) {
+    (void)E;
+    (void)nev;
+    if (threadIdx.x != 0) return;
+    const int t = J.tri[job], c = J.comp[job];
+    double re = V[0], im = V[1];
+    // orthocentre -> centroid (gamma.cu:83-91); Gamma1..3 conjugate phi1
+    double a1 = one_rotation_angle_otc(x2, x3, x1), a2 = one_rotation_angle_otc(x3, x1, x2),
+           a3 = one_rotation_angle_otc(x1, x2, x3);
+    if (c != 0) a1 = -a1;
+    double ang = -2. * (a1 + a2 + a3);
+    double cr = re * cos(ang) - im * sin(ang), ci = re * sin(ang) + im * cos(ang);
+    double om = cosm[cosmo].om;
+    double f = 27. / 8. * om * om * om * pow(100. / 299792., 5.0) / 3. / (2 * pow(2 * PI, 3.0));
+    out[8 * t + 2 * c] = cr * f;
+    out[8 * t + 2 * c + 1] = ci * f;
+    if (status && st) atomicOr(&status[t], st);
+  }
+};
+
+template <typename R, int NT>
+__global__ void __launch_bounds__(NT) k_gamma(GammaPolicy<R> pol_in, int njobs, int* job_counter, EngineCfg cfg,
+                                              char* scratch, size_t slot_bytes) {
+  GammaPolicy<R> pol = pol_in;
+  adaptive_body<3, 2, NT, GammaPolicy<R>>(pol, njobs, job_counter, cfg, scratch, slot_bytes);
+}
+
+template <typename R>
+static size_t gamma_smem_bytes() {
+  typedef GammaPolicy<R> P;
+  constexpr int NP = GMRule<3>::NP;
+  size_t b = (P::PSMEM + 15) & ~size_t(15);
+  b += ((size_t)P::CH * NP * P::REC + 15) & ~size_t(15);
+  b += sizeof(double) * (size_t)P::G * P::CH * NP * 2;
+  b += sizeof(double) * (size_t)P::CH * NP * 2;
+  b += sizeof(EngineShared<2>) + 16;
+  return b;
+}
+
+constexpr int GAMMA_NT = 256;
+
+template <typename R>
+static int run_gamma(tp_ctx* ctx, int cosmo, const double* d_x, const int* d_comp, const int* d_tri, int njobs,
+                     double rel_tol, double* d_out, int* d_status) {
+  size_t smem = gamma_smem_bytes<R>();
+  cudaError_t e =
+      cudaFuncSetAttribute(k_gamma<R, GAMMA_NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return tp_cuda(ctx, e, "gamma attribute");
+  int sms = 0, per_sm = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_gamma<R, GAMMA_NT>, GAMMA_NT, smem);
+  if (e != cudaSuccess || per_sm < 1) return tp_cuda(ctx, e == cudaSuccess ? cudaErrorInvalidConfiguration : e, "gamma occupancy");
+  int grid = sms * per_sm;
+  if (ctx->max_ctas > 0 && grid > ctx->max_ctas) grid = ctx->max_ctas;
+  if (grid > njobs) grid = njobs;
+  size_t slot = Slot<3, 2>::bytes(ctx->region_cap);
+  int st = ctx->ensure_scratch((size_t)grid * slot);
+  if (st) return st;
+  GammaPolicy<R> pol;
+  pol.J.x = d_x;
+  pol.J.comp = d_comp;
+  pol.J.tri = d_tri;
+  pol.tab = ctx->d_tab;
+  pol.cosm = ctx->d_cos;
+  pol.ck = (const CosmoK<R>*)(sizeof(R) == 8 ? ctx->d_ck64 : ctx->d_ck32);
+  pol.cosmo = cosmo;
+  pol.out = d_out;
+  pol.status = d_status;
+  EngineCfg cfg{0.0, rel_tol, TP_NORM_L1, ctx->region_cap, 2000};
+  e = cudaMemsetAsync(ctx->d_counter, 0, sizeof(int), ctx->stream);
+  if (e == cudaSuccess) {
+    k_gamma<R, GAMMA_NT><<<grid, GAMMA_NT, smem, ctx->stream>>>(pol, njobs, ctx->d_counter, cfg, ctx->d_scratch, slot);
+    e = cudaGetLastError();
+  }
+  return tp_cuda(ctx, e, "gamma launch");
+}
+
+}  // namespace tp
+
+using namespace tp;
+
+extern "C" int tp_ogata_weights(double* out) {
+  if (!out) return TP_ERR_ARG;
+  OgataTab o;
+  ogata_host(o);
+  for (int k = 0; k < PREC_K; ++k) {
+    out[k] = o.psi[0][k];
+    out[PREC_K + k] = k == 0 ? NAN : o.prod[0][k];
+    out[2 * PREC_K + k] = o.psi[1][k];
+    out[3 * PREC_K + k] = k == 0 ? NAN : o.prod[1][k];
+  }
+  return TP_OK;
+}
+
+extern "C" int tp_gamma_batch(tp_ctx* ctx, int cosmo_index, const double* x, int n, int comp_mask, double rel_tol,
+                              int precision, double* out, int* status_out) {
+  if (!ctx || !x || !out || n < 0 || (comp_mask & ~0xF) || comp_mask == 0) return TP_ERR_ARG;
+  if (precision != TP_FP64 && precision != TP_FP32) return TP_ERR_ARG;
+  if (!(rel_tol > 0)) return TP_ERR_ARG;
+  if (cosmo_index < 0 || cosmo_index >= ctx->n_cosmo) return tp_fail(ctx, TP_ERR_STATE, "no such cosmology");
+  for (int i = 0; i < 3 * n; ++i)
+    if (!(x[i] > 0)) return tp_fail(ctx, TP_ERR_ARG, "triangle sides must be > 0");
+  for (int t = 0; t < n; ++t) {
+    double a = x[3 * t], b = x[3 * t + 1], c = x[3 * t + 2];
+    if (a > b + c || b > a + c || c > a + b) return tp_fail(ctx, TP_ERR_ARG, "sides violate the triangle inequality");
+  }
+  if (n == 0) return TP_OK;
+  cudaSetDevice(ctx->device);
+  cudaError_t e = gamma_upload_constants();
+  if (e != cudaSuccess) return tp_cuda(ctx, e, "ogata constants");
+  std::vector<int> comp, tri;
+  for (int t = 0; t < n; ++t)
+    for (int c = 0; c < 4; ++c)
+      if (comp_mask & (1 << c)) {
+        comp.push_back(c);
+        tri.push_back(t);
+      }
+  const int nj = (int)comp.size();
+  size_t o_x = 0, o_c = (sizeof(double) * 3 * n + 255) & ~size_t(255);
+  size_t o_t = o_c + ((sizeof(int) * nj + 255) & ~size_t(255));
+  size_t o_o = o_t + ((sizeof(int) * nj + 255) & ~size_t(255));
+  size_t o_s = o_o + ((sizeof(double) * 8 * n + 255) & ~size_t(255));
+  int st = ctx->ensure_io(o_s + sizeof(int) * n + 256);
+  if (st) return st;
+  char* b = ctx->d_io;
+  cudaStream_t s = ctx->stream;
+  e = cudaMemcpyAsync(b + o_x, x, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(b + o_c, comp.data(), sizeof(int) * nj, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(b + o_t, tri.data(), sizeof(int) * nj, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(b + o_o, 0, sizeof(double) * 8 * n, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(b + o_s, 0, sizeof(int) * n, s);
+  if (e != cudaSuccess) return tp_cuda(ctx, e, "gamma upload");
+  st = precision == TP_FP64
+           ? run_gamma<double>(ctx, cosmo_index, (double*)(b + o_x), (int*)(b + o_c), (int*)(b + o_t), nj, rel_tol,
+                               (double*)(b + o_o), (int*)(b + o_s))
+           : run_gamma<float>(ctx, cosmo_index, (double*)(b + o_x), (int*)(b + o_c), (int*)(b + o_t), nj, rel_tol,
+                              (double*)(b + o_o), (int*)(b + o_s));
+  if (st) return st;
+  std::vector<int> hst(n);
+  e = cudaMemcpyAsync(out, b + o_o, sizeof(double) * 8 * n, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(hst.data(), b + o_s, sizeof(int) * n, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return tp_cuda(ctx, e, "gamma");
+  int bad = 0;
+  for (int t = 0; t < n; ++t) {
+    if (status_out) status_out[t] = hst[t];
+    bad += hst[t] != 0;
+  }
+  if (bad) return tp_fail(ctx, TP_ERR_CAPACITY, std::to_string(bad) + " Gamma integrals hit a region or sweep cap");
+  return TP_OK;
+}
