@@ -172,7 +172,15 @@ int tp_ogata_weights(double* out);
  * covarianceParameters (cosmology.cu:92-170). out[i] = T_term(th123[i], th456[i]). */
 int tp_cov_total_batch(tp_ctx* ctx, int cosmo_index, int term, int geometry, double theta_max, double area,
                        const double* th123, const double* th456, int n, int precision, double* out,
-                       int* status_out);
+                       int* n_capped);
+
+/* Single covariance terms T1(th1..th6), T2(th1..th6), T4(th1..th6)
+ * (apertureStatisticsCovariance.cu:1065-1197) for n six-tuples th6[n][6],
+ * without the permutation sums. T2 is 0 for the infinite geometry; T4 is
+ * evaluated in the infinite geometry normalised by area. *n_capped (optional)
+ * receives the number of integrals that hit a cap. */
+int tp_cov_term_batch(tp_ctx* ctx, int cosmo_index, int term, int geometry, double theta_max, double area,
+                      const double* th6, int n, int precision, double* out, int* n_capped);
 
 #ifdef __cplusplus
 }

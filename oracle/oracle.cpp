@@ -1350,7 +1350,9 @@ int integrand_T2_v(unsigned ndim, size_t npts, const double* x, void* fdata, uns
       double lx = x[i * ndim], ly = x[i * ndim + 1];
       double G = G_square(c->p->thetaMax, lx, ly);
       double ell = sqrt(lx * lx + ly * ly);
-      if (!(ell < c->p->lMin)) res = Pell(c->t, ell) * uHat(ell * c->th1) * uHat(ell * c->th2) * G;
+      // ell = 0 (the centre of the symmetric box) is the integrand's limit 0;
+      // the reference evaluates Pell(0) there, which is NaN
+      if (!(ell < c->p->lMin) && ell > 0) res = Pell(c->t, ell) * uHat(ell * c->th1) * uHat(ell * c->th2) * G;
     } else {  // circle
       double ell = x[i * ndim];
       if (!(ell < c->p->lMin))

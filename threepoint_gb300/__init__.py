@@ -104,6 +104,7 @@ def lib():
         L.tp_gamma_batch.argtypes = [p, i, dp, i, i, d, i, dp, ip]
         L.tp_ogata_weights.argtypes = [dp]
         L.tp_cov_total_batch.argtypes = [p, i, i, i, d, d, dp, dp, i, i, dp, ip]
+        L.tp_cov_term_batch.argtypes = [p, i, i, i, d, d, dp, i, i, dp, ip]
         _lib = L
     return _lib
 
@@ -314,13 +315,33 @@ class Context:
     # -- covariance (cuda_version/apertureStatisticsCovariance.cu:272-683) --
     def cov_total(self, term, th123, th456, geometry=GEOM_SQUARE, thetaMax=0.0, area=0.0, precision=FP64,
                   cosmo_index=0):
+        """T1_total / T2_total / T4_total for pairs of triplets
+        (apertureStatisticsCovariance.cu:272-683)."""
         a = _arr(th123).reshape(-1, 3)
         b = _arr(th456).reshape(-1, 3)
         out = np.zeros(len(a))
-        st = np.zeros(len(a), dtype=np.int32)
+        nb = C.c_int(0)
         _check(self._h, lib().tp_cov_total_batch(self._h, cosmo_index, term, geometry, thetaMax, area, _dp(a), _dp(b),
-                                                 len(a), precision, _dp(out), st.ctypes.data_as(C.POINTER(C.c_int))))
+                                                 len(a), precision, _dp(out), C.byref(nb)))
         return out
+
+    def cov_term(self, term, th6, geometry=GEOM_SQUARE, thetaMax=0.0, area=0.0, precision=FP64, cosmo_index=0):
+        """Single terms T1/T2/T4(theta1..theta6) (apertureStatisticsCovariance.cu:1065-1197)."""
+        t = _arr(th6).reshape(-1, 6)
+        out = np.zeros(len(t))
+        nb = C.c_int(0)
+        _check(self._h, lib().tp_cov_term_batch(self._h, cosmo_index, term, geometry, thetaMax, area, _dp(t), len(t),
+                                                precision, _dp(out), C.byref(nb)))
+        return out
+
+    def T1_total(self, th123, th456, **kw):
+        return float(self.cov_total(1, [th123], [th456], **kw)[0])
+
+    def T2_total(self, th123, th456, **kw):
+        return float(self.cov_total(2, [th123], [th456], **kw)[0])
+
+    def T4_total(self, th123, th456, **kw):
+        return float(self.cov_total(4, [th123], [th456], **kw)[0])
 
 
 def ogata_weights():

@@ -43,6 +43,7 @@ template <typename R>
 struct CosmoK {
   R omh2, sa, one_m_sa, sh043, theta2, l2theta2, c184, ehc, ns, alpha_max;
   R l2h;             // log2(h)
+  R h;
   int pk_given;
   R ln_kmin, inv_dk;  // tabulated P(k)
   const double* pk;   // 256 values (FP64, read through the cache)
@@ -62,6 +63,7 @@ __host__ __device__ inline CosmoK<R> make_cosmok(const EHConst& e, const CosmoDe
   k.ns = (R)e.ns;
   k.alpha_max = (R)(1. - (2. / 3.) * c.ns);
   k.l2h = (R)log2(c.h);
+  k.h = (R)c.h;
   k.pk_given = c.pk_given;
   k.ln_kmin = (R)(c.pk_given ? log(c.kmin) : 0.0);
   k.inv_dk = (R)(c.pk_given ? 1.0 / c.dk : 0.0);

@@ -213,6 +213,7 @@ void tp_ctx::free_cosmo() {
   cudaFree(d_ncoef64);
   cudaFree(d_ncoef32);
   cudaFree(d_hcoef);
+  cudaFree(d_hcoef32);
   cudaFree(d_wscale64);
   cudaFree(d_wscale32);
   cudaFree(d_ck64);
@@ -224,6 +225,7 @@ void tp_ctx::free_cosmo() {
   d_ncoef64 = nullptr;
   d_ncoef32 = nullptr;
   d_hcoef = nullptr;
+  d_hcoef32 = nullptr;
   d_wscale64 = d_wscale32 = nullptr;
   d_ck64 = nullptr;
   d_ck32 = nullptr;
@@ -347,6 +349,7 @@ extern "C" int tp_set_cosmologies(tp_ctx* ctx, const tp_cosmology* cosmo, int n,
     if (e == cudaSuccess) e = dalloc(&ctx->d_ncoef64, (size_t)cap * NC_COUNT * NNODE);
     if (e == cudaSuccess) e = dalloc(&ctx->d_ncoef32, (size_t)cap * NC_COUNT * NNODE);
     if (e == cudaSuccess) e = dalloc(&ctx->d_hcoef, (size_t)cap * HC_COUNT * NNODE);
+    if (e == cudaSuccess) e = dalloc(&ctx->d_hcoef32, (size_t)cap * HC_COUNT * NNODE);
     if (e == cudaSuccess) e = dalloc(&ctx->d_wscale64, cap);
     if (e == cudaSuccess) e = dalloc(&ctx->d_wscale32, cap);
     if (e == cudaSuccess) e = dalloc((CosmoK<double>**)&ctx->d_ck64, cap);
@@ -369,7 +372,7 @@ extern "C" int tp_set_cosmologies(tp_ctx* ctx, const tp_cosmology* cosmo, int n,
       e = cudaMemcpyAsync((char*)ctx->d_tab + (size_t)i * sizeof(TablesDev) + offsetof(TablesDev, pk), pk + (size_t)i * NK, sizeof(double) * NK, cudaMemcpyHostToDevice, s);
   if (e == cudaSuccess)
     e = build_tables(ctx->d_cos, ctx->d_eh, ctx->d_nz, nz_stride, ctx->d_tab, ctx->d_ncoef64, ctx->d_ncoef32,
-                     ctx->d_hcoef, ctx->d_wscale64, ctx->d_wscale32, (CosmoK<double>*)ctx->d_ck64,
+                     ctx->d_hcoef, ctx->d_hcoef32, ctx->d_wscale64, ctx->d_wscale32, (CosmoK<double>*)ctx->d_ck64,
                      (CosmoK<float>*)ctx->d_ck32, n, s);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);
   if (e != cudaSuccess) return tp_cuda(ctx, e, "table build");

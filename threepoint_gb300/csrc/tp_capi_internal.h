@@ -26,6 +26,7 @@ struct tp_ctx {
   double* d_ncoef64 = nullptr;
   float* d_ncoef32 = nullptr;
   double* d_hcoef = nullptr;
+  float* d_hcoef32 = nullptr;
   double* d_wscale64 = nullptr;
   double* d_wscale32 = nullptr;
   void* d_ck64 = nullptr;

@@ -309,15 +309,24 @@ template <int FDIM>
 struct EngineShared {
   int live_list[1024];  // live points of the current chunk
   int nlive_chunk;
-  double hist[256];
+  unsigned long long hist[256];
   double red[64];
   int ired[80];
   double V[FDIM], E[FDIM];
-  double s_above;
+  unsigned long long q_above;
   unsigned long long prefix;
   int job, nlive, npend, status, stop, ktot, sweeps;
   long long neval;
 };
+
+// Dynamic shared memory of adaptive_body for policy P.
+template <int DIM, int FDIM, class P>
+__host__ __device__ constexpr size_t engine_smem_bytes() {
+  return ((P::PSMEM + 15) & ~size_t(15)) + (((size_t)P::CH * GMRule<DIM>::NP * P::REC + 15) & ~size_t(15)) +
+         sizeof(double) * (size_t)P::G * P::CH * GMRule<DIM>::NP * P::PD +
+         sizeof(double) * (size_t)P::CH * GMRule<DIM>::NP * FDIM + sizeof(EngineShared<FDIM>) + 16;
+}
+
 
 // ---------------------------------------------------------------------------
 // The persistent adaptive-integration kernel body. Policy P provides:
@@ -325,7 +334,8 @@ struct EngineShared {
 //   __device__ void begin_job(int job, char* psmem, double* xmin, double* xmax) (all threads; syncs inside)
 //   __device__ bool setup(int p, const double* x, char* rec)   (true: point needs its groups)
 //   __device__ bool is_live(const char* rec)
-//   __device__ void group(const char* rec, int g, double* part /*FDIM*/)  (live points only)
+//   __device__ void group(const char* rec, int g, double* part /*PD*/)  (live points only)
+//   static int slot(int g): sum class of group g (0..NS-1)
 //   __device__ void finalize(const char* rec, const double* sum /*FDIM*/, double* fval /*FDIM*/)
 //   __device__ void end_job(int job, const double* V, const double* E, long long neval, int status)
 //   static constexpr size_t PSMEM (policy shared bytes)
@@ -335,12 +345,14 @@ __device__ void adaptive_body(P& pol, int njobs, int* job_counter, const EngineC
   constexpr int NP = GMRule<DIM>::NP;
   constexpr int CH = P::CH;
   constexpr int G = P::G;
+  constexpr int PD = P::PD;  // values per group item (>= 1)
+  constexpr int NS = P::NS;  // group classes: item g adds into sum class P::slot(g)
   static_assert(P::CH * NP <= 1024, "live list holds one chunk");
   extern __shared__ __align__(16) char smem[];
   char* psmem = smem;
   char* recs = psmem + ((P::PSMEM + 15) & ~size_t(15));
-  double* part = (double*)(recs + (((size_t)CH * NP * P::REC + 15) & ~size_t(15)));  // [G][CH*NP][FDIM]
-  double* fval = part + (size_t)G * CH * NP * FDIM;                               // [CH*NP][FDIM]
+  double* part = (double*)(recs + (((size_t)CH * NP * P::REC + 15) & ~size_t(15)));  // [G][CH*NP][PD]
+  double* fval = part + (size_t)G * CH * NP * PD;                                 // [CH*NP][FDIM]
   EngineShared<FDIM>* es = (EngineShared<FDIM>*)(fval + (size_t)CH * NP * FDIM);
 
   Slot<DIM, FDIM> S;
@@ -398,21 +410,23 @@ __device__ void adaptive_body(P& pol, int njobs, int* job_counter, const EngineC
         for (int it = tid; it < nl * G; it += NT) {
           int g = it / nl, q = it - g * nl;
           int p = es->live_list[q];
-          double pv[FDIM];
+          double pv[PD];
           pol.group(recs + (size_t)p * P::REC, g, pv);
 #pragma unroll
-          for (int k = 0; k < FDIM; ++k) part[((size_t)g * npts + p) * FDIM + k] = pv[k];
+          for (int k = 0; k < PD; ++k) part[((size_t)g * npts + p) * PD + k] = pv[k];
         }
         __syncthreads();
         // (c) per-point totals (fixed group order -> deterministic)
         for (int p = tid; p < npts; p += NT) {
-          double s[FDIM];
+          double s[NS * PD];
 #pragma unroll
-          for (int k = 0; k < FDIM; ++k) s[k] = 0;
+          for (int k = 0; k < NS * PD; ++k) s[k] = 0;
           if (pol.is_live(recs + (size_t)p * P::REC))
-            for (int g = 0; g < G; ++g)
+            for (int g = 0; g < G; ++g) {
+              const int sl = P::slot(g);
 #pragma unroll
-              for (int k = 0; k < FDIM; ++k) s[k] += part[((size_t)g * npts + p) * FDIM + k];
+              for (int k = 0; k < PD; ++k) s[sl * PD + k] += part[((size_t)g * npts + p) * PD + k];
+            }
           pol.finalize(recs + (size_t)p * P::REC, s, fval + (size_t)p * FDIM);
         }
         if (tid == 0) es->nlive_chunk = 0;
@@ -477,13 +491,18 @@ __device__ void adaptive_body(P& pol, int njobs, int* job_counter, const EngineC
         tol = fmax(cfg.abs_tol, fabs(tv[0]) * cfg.rel_tol);
 
       // ---------------- radix select of the error threshold ---------------
+      // Errors are summed as 62-bit fixed-point fractions of the total error,
+      // so the histogram sums (shared-memory integer atomics) are exact and
+      // independent of the order of the additions.
+      const double qscale = 4.611686018427387904e18 / etot;  // 2^62 / E_tot
+      const double tol_q = tol * qscale;
       if (tid == 0) {
         es->prefix = 0ull;
-        es->s_above = 0.0;
+        es->q_above = 0ull;
       }
       for (int pass = 0; pass < 8; ++pass) {
         const int shift = 56 - 8 * pass;
-        for (int b = tid; b < 256; b += NT) es->hist[b] = 0.0;
+        for (int b = tid; b < 256; b += NT) es->hist[b] = 0ull;
         __syncthreads();
         const unsigned long long pre = es->prefix;
         for (int i = tid; i < nlive; i += NT) {
@@ -492,55 +511,58 @@ __device__ void adaptive_body(P& pol, int njobs, int* job_counter, const EngineC
             double es_ = 0;
 #pragma unroll
             for (int k = 0; k < FDIM; ++k) es_ += S.err[(size_t)k * S.cap + i];
-            atomicAdd(&es->hist[(key >> shift) & 255ull], es_);
+            atomicAdd(&es->hist[(key >> shift) & 255ull], (unsigned long long)(es_ * qscale));
           }
         }
         __syncthreads();
         if (tid < 32) {
           const int l = tid;
-          double loc[8];
-          double ls = 0;
+          unsigned long long loc[8];
+          unsigned long long ls = 0;
 #pragma unroll
           for (int q = 0; q < 8; ++q) {
             loc[q] = es->hist[8 * l + q];
             ls += loc[q];
           }
+          // pass 0 histograms every region: its sum is the fixed-point total
+          unsigned long long tot = ls;
+          for (int o = 16; o > 0; o >>= 1) tot += __shfl_xor_sync(0xffffffffu, tot, o);
+          __shared__ unsigned long long s_qtot;
+          if (pass == 0 && l == 0) s_qtot = tot;
+          __syncwarp();
+          const unsigned long long qtot = s_qtot;
           // suffix sum over lanes (lane l: sum of lanes > l)
-          double suf = ls;
+          unsigned long long suf = ls;
           for (int o = 1; o < 32; o <<= 1) {
-            double y = __shfl_down_sync(0xffffffffu, suf, o);
+            unsigned long long y = __shfl_down_sync(0xffffffffu, suf, o);
             if (l + o < 32) suf += y;
           }
-          double above_lane = suf - ls;  // sum of bins in lanes > l
-          double cum = es->s_above + above_lane;
+          unsigned long long cum = es->q_above + (suf - ls);
           int best = -1;
-          double cum_best = 0;
+          unsigned long long cum_best = 0;
 #pragma unroll
           for (int q = 7; q >= 0; --q) {
             cum += loc[q];
-            if (best < 0 && etot - cum <= tol) {
+            if (best < 0 && (double)(qtot > cum ? qtot - cum : 0ull) <= tol_q) {
               best = 8 * l + q;
               cum_best = cum;
             }
           }
           int chosen = __reduce_max_sync(0xffffffffu, best);
-          if (chosen < 0) chosen = 0;
-          // S_above for the next pass: everything in bins strictly above chosen
-          double cb = (best == chosen) ? cum_best : 0.0;
-          double hb = (best == chosen) ? es->hist[chosen] : 0.0;
+          bool none = chosen < 0;
+          if (none) chosen = 0;
+          unsigned long long cb = (best == chosen && !none) ? cum_best : 0ull;
+          unsigned long long hb = (best == chosen && !none) ? es->hist[chosen] : 0ull;
           for (int o = 16; o > 0; o >>= 1) {
             cb += __shfl_xor_sync(0xffffffffu, cb, o);
             hb += __shfl_xor_sync(0xffffffffu, hb, o);
           }
+          unsigned long long all = ls;
+          for (int o = 16; o > 0; o >>= 1) all += __shfl_xor_sync(0xffffffffu, all, o);
           if (l == 0) {
-            if (best < 0 && chosen == 0) {
-              // no bin satisfies (rounding): take the whole current range
-              double all = 0;
-              for (int b = 0; b < 256; ++b) all += es->hist[b];
-              es->s_above = es->s_above + all - es->hist[0];
-            } else {
-              es->s_above = cb - hb;
-            }
+            // bins strictly above the chosen one are selected for sure; when no
+            // bin satisfies the tolerance (rounding), take the whole range
+            es->q_above = none ? es->q_above + all - es->hist[0] : cb - hb;
             es->prefix = (pre << 8) | (unsigned long long)chosen;
           }
         }

@@ -116,6 +116,9 @@ struct GammaPolicy {
     int live;
   };
   static constexpr int REC = (int)sizeof(Rec);
+  static constexpr int PD = 2;
+  static constexpr int NS = 1;
+  __device__ static int slot(int) { return 0; }
   static constexpr size_t PSMEM = sizeof(CosmoK<R>) + 64;
 
   GammaJobs J;

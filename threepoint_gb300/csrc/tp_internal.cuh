@@ -74,6 +74,9 @@ enum HaloCoef {
   HC_D1SQ,     // D1^2
   HC_A, HC_B, HC_C, HC_GAM, HC_ALPHA, HC_BETA, HC_XNU,
   HC_F1, HC_F2, HC_F3,
+  HC_L2INVFK,  // log2(1/f_K)
+  HC_L2RS,     // log2(r_sigma)
+  HC_L2F3C,    // log2(f3 * c)
   HC_COUNT
 };
 

@@ -30,6 +30,9 @@ struct Map3Policy {
     int live;
   };
   static constexpr int REC = (int)sizeof(Rec);
+  static constexpr int PD = 1;
+  static constexpr int NS = 1;
+  __device__ static int slot(int) { return 0; }
   static constexpr size_t PSMEM = sizeof(R) * NC_COUNT * NNODE + sizeof(CosmoK<R>) + sizeof(BulkBar) + 128;
 
   // inputs

@@ -319,7 +319,7 @@ __device__ inline double interp_mid(const double* arr, double zfrac_bins) {
 // integrand_bkappa + bispec, bispectrum.cu:221-333) and of P_kappa's
 // (limber_integrand_power_spectrum + P_k_nonlinear, bispectrum.cu:531-600,951-991).
 __global__ void k_node_coefs(const CosmoDev* cos, const TablesDev* tab, double* ncoef, float* ncoef_f, double* hcoef,
-                             int n) {
+                             float* hcoef_f, int n) {
   int ci = blockIdx.x;
   int j = threadIdx.x;
   if (ci >= n || j >= NNODE) return;
@@ -409,8 +409,15 @@ __global__ void k_node_coefs(const CosmoDev* cos, const TablesDev* tab, double* 
     v[HC_F1] = frac * f1b + (1 - frac) * f1a;
     v[HC_F2] = frac * f2b + (1 - frac) * f2a;
     v[HC_F3] = frac * f3b + (1 - frac) * f3a;
+    v[HC_L2INVFK] = log2(1.0 / fK);
+    v[HC_L2RS] = log2(rs);
+    v[HC_L2F3C] = log2(v[HC_F3] * v[HC_C]);
     double* o = hcoef + (size_t)ci * HC_COUNT * NNODE;
-    for (int q = 0; q < HC_COUNT; ++q) o[q * NNODE + j] = v[q];
+    float* of = hcoef_f + (size_t)ci * HC_COUNT * NNODE;
+    for (int q = 0; q < HC_COUNT; ++q) {
+      o[q * NNODE + j] = v[q];
+      of[q * NNODE + j] = (float)v[q];
+    }
   }
 }
 
@@ -448,15 +455,15 @@ void upload_gauss_nodes() {
 }
 
 cudaError_t build_tables(const CosmoDev* d_cos, EHConst* d_eh, const double* d_nz, int nz_stride, TablesDev* d_tab,
-                         double* d_ncoef, float* d_ncoef_f, double* d_hcoef, double* d_wscale64, double* d_wscale32,
-                         CosmoK<double>* d_ck64, CosmoK<float>* d_ck32, int n, cudaStream_t s) {
+                         double* d_ncoef, float* d_ncoef_f, double* d_hcoef, float* d_hcoef_f, double* d_wscale64,
+                         double* d_wscale32, CosmoK<double>* d_ck64, CosmoK<float>* d_ck32, int n, cudaStream_t s) {
   k_norm<<<n, 32, 0, s>>>(d_cos, d_eh, d_tab, n);
   k_fk_g<<<n, 256, 0, s>>>(d_cos, d_nz, nz_stride, d_tab, n);
   k_growth<<<n, NZ + 32, 0, s>>>(d_cos, d_tab, n);
   long warps = (long)n * NZ;
   int wpb = 4;
   k_rsigma<<<(unsigned)((warps + wpb - 1) / wpb), 32 * wpb, 0, s>>>(d_cos, d_eh, d_tab, n);
-  k_node_coefs<<<n, NNODE, 0, s>>>(d_cos, d_tab, d_ncoef, d_ncoef_f, d_hcoef, n);
+  k_node_coefs<<<n, NNODE, 0, s>>>(d_cos, d_tab, d_ncoef, d_ncoef_f, d_hcoef, d_hcoef_f, n);
   k_finish<<<n, NNODE, 0, s>>>(d_cos, d_eh, d_tab, d_ncoef, d_ncoef_f, d_wscale64, d_wscale32, d_ck64, d_ck32, n);
   return cudaGetLastError();
 }
