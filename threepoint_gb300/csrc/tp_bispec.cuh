@@ -47,6 +47,7 @@ struct CosmoK {
   int pk_given;
   R ln_kmin, inv_dk;  // tabulated P(k)
   const double* pk;   // 256 values (FP64, read through the cache)
+  const float* plt;   // log2 P_lin cubic segments (PLT_N float4) for the FP32 path, or null
 };
 
 template <typename R>
@@ -68,6 +69,7 @@ __host__ __device__ inline CosmoK<R> make_cosmok(const EHConst& e, const CosmoDe
   k.ln_kmin = (R)(c.pk_given ? log(c.kmin) : 0.0);
   k.inv_dk = (R)(c.pk_given ? 1.0 / c.dk : 0.0);
   k.pk = pk_dev;
+  k.plt = nullptr;
   return k;
 }
 
@@ -84,6 +86,17 @@ __device__ __forceinline__ R plin(const CosmoK<R>& K, R kk, R l2kk) {
     int idx = (int)didx;
     R f = didx - (R)idx;
     return (R)K.pk[idx] * ((R)1 - f) + (R)K.pk[idx + 1] * f;
+  }
+  if constexpr (sizeof(R) == 4) {
+    if (K.plt) {
+      const float inv = (float)((PLT_N - 1) / (PLT_HI - PLT_LO));
+      float t = (l2kk - (float)PLT_LO) * inv;
+      t = fminf(fmaxf(t, 0.f), (float)(PLT_N - 1) - 1e-3f);
+      int i = (int)t;
+      float f = t - (float)i;
+      const float4 q = reinterpret_cast<const float4*>(K.plt)[i];
+      return M::ex2(q.x + f * (q.y + f * (q.z + f * q.w)));
+    }
   }
   R x = kk * K.sh043;
   R x2 = x * x;
@@ -224,12 +237,27 @@ __device__ __forceinline__ R bispec_eval(const R* __restrict__ nc, int stride, R
   return bs1h + bs3h;
 }
 
-// B(ell_i / f_K(z_j), z_j) at line-of-sight node j of a node table
-// (coef c of node j at nc[c*NNODE + j]).
+// B(ell_i / f_K(z_j), z_j) at line-of-sight node j of a node table stored
+// node-major (coef c of node j at nc[j*NCP + c]); the FP32 row is fetched with
+// 16-byte vector loads.
 template <typename R>
 __device__ __forceinline__ R bispec_node(const R* __restrict__ nc, int j, const Tri<R>& T, const CosmoK<R>& K) {
-  return bispec_eval<R>(nc + j, NNODE, nc[NC_S * NNODE + j], nc[NC_L2S * NNODE + j], nc[NC_HF * NNODE + j],
-                        nc[NC_L2HF * NNODE + j], T, K);
+  const R* row = nc + j * NCP;
+  if constexpr (sizeof(R) == 4) {
+    float c[NCP];
+    const float4* v = reinterpret_cast<const float4*>(row);
+#pragma unroll
+    for (int q = 0; q < NCP / 4; ++q) {
+      float4 t = v[q];
+      c[4 * q] = t.x;
+      c[4 * q + 1] = t.y;
+      c[4 * q + 2] = t.z;
+      c[4 * q + 3] = t.w;
+    }
+    return c[NC_W] * bispec_eval<float>(c, 1, c[NC_S], c[NC_L2S], c[NC_HF], c[NC_L2HF], T, K);
+  } else {
+    return row[NC_W] * bispec_eval<R>(row, 1, row[NC_S], row[NC_L2S], row[NC_HF], row[NC_L2HF], T, K);
+  }
 }
 
 // Mid-bin two-point interpolation of a z table at fractional bin position fb

@@ -31,6 +31,7 @@ struct tp_ctx {
   double* d_wscale32 = nullptr;
   void* d_ck64 = nullptr;
   void* d_ck32 = nullptr;
+  float4* d_plt = nullptr;  // [n_cosmo][PLT_N] log2 P_lin cubic segments
 
   // shape noise of P(ell)
   double sigma_eps = 0.0, ngal = 1.0;

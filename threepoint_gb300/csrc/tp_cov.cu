@@ -253,7 +253,7 @@ struct BkProd {
     int valid;
   };
   static constexpr int REC = (int)sizeof(Rec);
-  static constexpr size_t PSMEM = sizeof(R) * NC_COUNT * NNODE + sizeof(CosmoK<R>) + 64;
+  static constexpr size_t PSMEM = sizeof(R) * NCP * NNODE + sizeof(CosmoK<R>) + 64;
 
   const CovJob* jobs;
   const R* ncoef;
@@ -270,7 +270,7 @@ struct BkProd {
     s_nc = (R*)psmem;
     if (!loaded) {
       __syncthreads();
-      for (int i = threadIdx.x; i < NC_COUNT * NNODE; i += blockDim.x) s_nc[i] = ncoef[i];
+      for (int i = threadIdx.x; i < NCP * NNODE; i += blockDim.x) s_nc[i] = ncoef[i];
       __syncthreads();
       loaded = 1;
     }
@@ -319,7 +319,7 @@ struct BkProd {
     const int j0 = ch * 12;
 #pragma unroll 2
     for (int j = j0; j < j0 + 12; ++j) {
-      R v = s_nc[NC_W * NNODE + j] * bispec_node<R>(s_nc, j, r.t[i], ck);
+      R v = bispec_node<R>(s_nc, j, r.t[i], ck);
       if (v != v) v = (R)0;
       acc.add(v);
     }
@@ -561,7 +561,7 @@ static int run_t4(tp_ctx* ctx, int cosmo, const JobSet& js, double norm, std::ve
   memset(&pol, 0, sizeof(pol));
   pol.jobs = (const CovJob*)(b + o_j);
   pol.ncoef = (sizeof(R) == 8 ? (const R*)(const void*)ctx->d_ncoef64 : (const R*)(const void*)ctx->d_ncoef32) +
-              (size_t)cosmo * NC_COUNT * NNODE;
+              (size_t)cosmo * NCP * NNODE;
   CosmoK<R> ck;
   double ws = 1.0;
   if (e == cudaSuccess)

@@ -17,6 +17,12 @@ constexpr double C_OVER_H0 = 2997.92;
 constexpr double PI = 3.14159265358979323846;
 constexpr double LOG2_10 = 3.32192809488736234787;
 constexpr double LN2 = 0.69314718055994530942;
+// FP32 integrands read the Eisenstein & Hu linear P(k) from a per-cosmology
+// table of log2 P on a uniform log2(k h) grid, interpolated by Catmull-Rom
+// cubics (relative error ~1e-6 over the grid); FP64 integrands evaluate the
+// fit itself.
+constexpr int PLT_N = 1024;  // grid points; the table stores per interval (y0, c1, c2, c3) of the cubic
+constexpr double PLT_LO = -24.0, PLT_HI = 24.0;
 
 // Per-cosmology parameter block as uploaded to the device.
 struct CosmoDev {
@@ -64,6 +70,9 @@ enum NodeCoef {
   NC_D1P4,     // D1^4 (tree level)
   NC_COUNT
 };
+// node tables are stored node-major with this pitch (16-byte rows for float4 loads)
+constexpr int NCP = 28;
+static_assert(NC_COUNT <= NCP, "node coefficient pitch");
 
 // Per-node Halofit coefficients for the P_kappa line-of-sight integral
 // (P_k_nonlinear + limber prefactor at the fixed nodes; z-only parts).

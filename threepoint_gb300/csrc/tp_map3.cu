@@ -33,7 +33,8 @@ struct Map3Policy {
   static constexpr int PD = 1;
   static constexpr int NS = 1;
   __device__ static int slot(int) { return 0; }
-  static constexpr size_t PSMEM = sizeof(R) * NC_COUNT * NNODE + sizeof(CosmoK<R>) + sizeof(BulkBar) + 128;
+  static constexpr size_t PLT_BYTES = sizeof(R) == 4 ? sizeof(float4) * PLT_N : 0;
+  static constexpr size_t PSMEM = sizeof(R) * NCP * NNODE + sizeof(CosmoK<R>) + sizeof(BulkBar) + 128 + PLT_BYTES;
 
   // inputs
   const int* job_cosmo;
@@ -58,28 +59,40 @@ struct Map3Policy {
   double scale;
 
   __device__ BulkBar* bar(char* psmem) {
-    return (BulkBar*)(psmem + sizeof(R) * NC_COUNT * NNODE + ((sizeof(CosmoK<R>) + 15) & ~size_t(15)));
+    return (BulkBar*)(psmem + sizeof(R) * NCP * NNODE + ((sizeof(CosmoK<R>) + 15) & ~size_t(15)));
   }
   __device__ unsigned long long* live_counter(char* psmem) {
     return (unsigned long long*)((char*)bar(psmem) + ((sizeof(BulkBar) + 15) & ~size_t(15)));
   }
+  __device__ float4* plt_smem(char* psmem) { return (float4*)((char*)live_counter(psmem) + 16); }
   unsigned long long* s_live;
 
   __device__ void begin_job(int job, char* psmem, double* xmin, double* xmax) {
     s_nc = (R*)psmem;
-    s_ck = (CosmoK<R>*)(psmem + sizeof(R) * NC_COUNT * NNODE);
+    s_ck = (CosmoK<R>*)(psmem + sizeof(R) * NCP * NNODE);
     const int c = job_cosmo[job];
     if (c != cur_cosmo) {
       __syncthreads();
-      const R* src = node_coef + (size_t)c * NC_COUNT * NNODE;
-      constexpr int nbytes = (int)(sizeof(R) * NC_COUNT * NNODE);
+      const R* src = node_coef + (size_t)c * NCP * NNODE;
+      constexpr int nbytes = (int)(sizeof(R) * NCP * NNODE);
       static_assert(nbytes % 16 == 0, "bulk copy size must be a multiple of 16 bytes");
       if (threadIdx.x == 0) {
         // the node table (10-20 KB) is staged by one bulk async copy
         if (!bulk_copy_g2s(bar(psmem), s_nc, src, nbytes)) {
-          for (int i = 0; i < NC_COUNT * NNODE; ++i) s_nc[i] = src[i];
+          for (int i = 0; i < NCP * NNODE; ++i) s_nc[i] = src[i];
         }
         *s_ck = ck[c];
+      }
+      __syncthreads();
+      if constexpr (sizeof(R) == 4) {
+        // the FP32 linear-P(k) table follows the node table into shared memory
+        const float4* gp = reinterpret_cast<const float4*>(s_ck->plt);
+        if (gp) {
+          float4* sp = plt_smem(psmem);
+          for (int i = threadIdx.x; i < PLT_N; i += blockDim.x) sp[i] = gp[i];
+          __syncthreads();
+          if (threadIdx.x == 0) s_ck->plt = reinterpret_cast<const float*>(sp);
+        }
       }
       __syncthreads();
       cur_cosmo = c;
@@ -154,8 +167,7 @@ struct Map3Policy {
     const int j0 = g * NPG;
 #pragma unroll 2
     for (int j = j0; j < j0 + NPG; ++j) {
-      R b = bispec_node<R>(s_nc, j, r.tri, K);
-      R v = s_nc[NC_W * NNODE + j] * b;
+      R v = bispec_node<R>(s_nc, j, r.tri, K);
       if (v != v) v = (R)0;  // NaN in bispec -> 0 (bispectrum.cu:327-331)
       acc.add(v);
     }
@@ -182,7 +194,7 @@ struct Map3Policy {
 };
 
 template <typename R, int NT>
-__global__ void __launch_bounds__(NT) k_map3(Map3Policy<R> pol_in, int njobs, int* job_counter, EngineCfg cfg,
+__global__ void __launch_bounds__(NT, sizeof(R) == 4 ? 3 : 1) k_map3(Map3Policy<R> pol_in, int njobs, int* job_counter, EngineCfg cfg,
                                              char* scratch, size_t slot_bytes) {
   Map3Policy<R> pol = pol_in;
   pol.cur_cosmo = -1;
@@ -223,11 +235,11 @@ __global__ void k_bkappa_points(const int* cosmo_idx, const double* ell, long n,
   }
   Tri<R> T;
   make_tri<R>(l1, l2, l3, T);
-  const R* nc = node_coef + (size_t)c * NC_COUNT * NNODE;
+  const R* nc = node_coef + (size_t)c * NCP * NNODE;
   const CosmoK<R> K = ck[c];
   KSum<R> acc;
   for (int j = lane; j < NNODE; j += 32) {
-    R v = nc[NC_W * NNODE + j] * bispec_node<R>(nc, j, T, K);
+    R v = bispec_node<R>(nc, j, T, K);
     if (v != v) v = (R)0;
     acc.add(v);
   }

@@ -369,11 +369,11 @@ __global__ void k_node_coefs(const CosmoDev* cos, const TablesDev* tab, double* 
     v[NC_D1SQ] = D1 * D1;
     v[NC_TREE] = z > 10. ? 1.0 : 0.0;
     v[NC_D1P4] = D1 * D1 * D1 * D1;
-    double* o = ncoef + (size_t)ci * NC_COUNT * NNODE;
-    float* of = ncoef_f + (size_t)ci * NC_COUNT * NNODE;
-    for (int q = 0; q < NC_COUNT; ++q) {
-      o[q * NNODE + j] = v[q];
-      of[q * NNODE + j] = (float)v[q];
+    double* o = ncoef + ((size_t)ci * NNODE + j) * NCP;
+    float* of = ncoef_f + ((size_t)ci * NNODE + j) * NCP;
+    for (int q = 0; q < NCP; ++q) {
+      o[q] = q < NC_COUNT ? v[q] : 0.0;
+      of[q] = q < NC_COUNT ? (float)v[q] : 0.f;
     }
   }
   // ---- P_kappa nodes: interpolation index z/zmax*255 (bispectrum.cu:535,956)
@@ -431,8 +431,8 @@ __global__ void k_finish(const CosmoDev* cos, const EHConst* eh, const TablesDev
   __shared__ double wmax;
   if (threadIdx.x == 0) {
     double m = 0;
-    const double* W = ncoef + (size_t)ci * NC_COUNT * NNODE + NC_W * NNODE;
-    for (int j = 0; j < NNODE; ++j) m = fmax(m, fabs(W[j]));
+    const double* W = ncoef + (size_t)ci * NCP * NNODE + NC_W;
+    for (int j = 0; j < NNODE; ++j) m = fmax(m, fabs(W[j * NCP]));
     wmax = m > 0 ? m : 1.0;
     wscale64[ci] = 1.0;
     wscale32[ci] = wmax;
@@ -441,9 +441,34 @@ __global__ void k_finish(const CosmoDev* cos, const EHConst* eh, const TablesDev
   }
   __syncthreads();
   for (int j = threadIdx.x; j < NNODE; j += blockDim.x) {
-    size_t o = (size_t)ci * NC_COUNT * NNODE + NC_W * NNODE + j;
+    size_t o = ((size_t)ci * NNODE + j) * NCP + NC_W;
     ncoef_f[o] = (float)(ncoef[o] / wmax);
   }
+}
+
+// log2 P_lin on the FP32 interpolation grid (log2(k h) uniform on [PLT_LO, PLT_HI])
+// and its Catmull-Rom cubic per interval i: y(i + f) = y0 + f (c1 + f (c2 + f c3))
+__global__ void k_plin_table(const CosmoDev* cos, const EHConst* eh, float4* plt, CosmoK<float>* ck32, int n) {
+  int ci = blockIdx.x;
+  if (ci >= n) return;
+  const CosmoDev c = cos[ci];
+  const EHConst e = eh[ci];
+  __shared__ double y[PLT_N + 2];
+  for (int i = threadIdx.x; i < PLT_N + 2; i += blockDim.x) {
+    double kk = exp2(PLT_LO + (i - 1) * (PLT_HI - PLT_LO) / (PLT_N - 1));
+    y[i] = log2(eh_linear_pk(e, kk / c.h));
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < PLT_N; i += blockDim.x) {
+    double ym1 = y[i], y0 = y[i + 1], y1 = y[i + 2], y2 = i + 3 < PLT_N + 2 ? y[i + 3] : y[i + 2];
+    float4 q;
+    q.x = (float)y0;
+    q.y = (float)(0.5 * (y1 - ym1));
+    q.z = (float)(0.5 * (2 * ym1 - 5 * y0 + 4 * y1 - y2));
+    q.w = (float)(0.5 * (3 * (y0 - y1) + y2 - ym1));
+    plt[(size_t)ci * PLT_N + i] = q;
+  }
+  if (threadIdx.x == 0 && !c.pk_given) ck32[ci].plt = (const float*)(plt + (size_t)ci * PLT_N);
 }
 
 // ---------------------------------------------------------------------------
@@ -456,7 +481,8 @@ void upload_gauss_nodes() {
 
 cudaError_t build_tables(const CosmoDev* d_cos, EHConst* d_eh, const double* d_nz, int nz_stride, TablesDev* d_tab,
                          double* d_ncoef, float* d_ncoef_f, double* d_hcoef, float* d_hcoef_f, double* d_wscale64,
-                         double* d_wscale32, CosmoK<double>* d_ck64, CosmoK<float>* d_ck32, int n, cudaStream_t s) {
+                         double* d_wscale32, CosmoK<double>* d_ck64, CosmoK<float>* d_ck32, float4* d_plt, int n,
+                         cudaStream_t s) {
   k_norm<<<n, 32, 0, s>>>(d_cos, d_eh, d_tab, n);
   k_fk_g<<<n, 256, 0, s>>>(d_cos, d_nz, nz_stride, d_tab, n);
   k_growth<<<n, NZ + 32, 0, s>>>(d_cos, d_tab, n);
@@ -465,6 +491,7 @@ cudaError_t build_tables(const CosmoDev* d_cos, EHConst* d_eh, const double* d_n
   k_rsigma<<<(unsigned)((warps + wpb - 1) / wpb), 32 * wpb, 0, s>>>(d_cos, d_eh, d_tab, n);
   k_node_coefs<<<n, NNODE, 0, s>>>(d_cos, d_tab, d_ncoef, d_ncoef_f, d_hcoef, d_hcoef_f, n);
   k_finish<<<n, NNODE, 0, s>>>(d_cos, d_eh, d_tab, d_ncoef, d_ncoef_f, d_wscale64, d_wscale32, d_ck64, d_ck32, n);
+  k_plin_table<<<n, 256, 0, s>>>(d_cos, d_eh, d_plt, d_ck32, n);
   return cudaGetLastError();
 }
 

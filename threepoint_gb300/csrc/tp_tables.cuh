@@ -13,6 +13,7 @@ void upload_gauss_nodes();
 // make_eh_const(c, 1.0) on entry; its ehc is rescaled by norm^2 on exit.
 cudaError_t build_tables(const CosmoDev* d_cos, EHConst* d_eh, const double* d_nz, int nz_stride, TablesDev* d_tab,
                          double* d_ncoef, float* d_ncoef_f, double* d_hcoef, float* d_hcoef_f, double* d_wscale64,
-                         double* d_wscale32, CosmoK<double>* d_ck64, CosmoK<float>* d_ck32, int n, cudaStream_t s);
+                         double* d_wscale32, CosmoK<double>* d_ck64, CosmoK<float>* d_ck32, float4* d_plt, int n,
+                         cudaStream_t s);
 
 }  // namespace tp
