@@ -170,6 +170,8 @@ def run_ours(args):
         off = ((rank * (args.steps + args.warmup) + step) * C) % (N_LHS - C)
         return [tp.cosmology(**c) for c in cosmos_all[off:off + C]]
 
+    order = [None]
+
     def one_step(step, timing):
         batch = cosmo_batch(step)
         ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
@@ -178,14 +180,21 @@ def run_ours(args):
             ctx.set_cosmologies(batch, nz)
             ev[1].record(stream)
             ctx.map3_jobs_device(job_cosmo, job_theta, out, err, nev, status, lMax=lmax, rel_tol=1e-4,
-                                 precision=tp.FP32, nlive=nlive)
+                                 precision=tp.FP32, nlive=nlive, job_order=order[0])
             ev[2].record(stream)
         if timing is not None:
             timing.append(ev)
 
-    # warm-up
+    # warm-up; after the first warm-up step the jobs are ordered longest-first
+    # by the per-triplet cost seen there (what tp_map3_batch does internally)
     for s in range(args.warmup):
         one_step(s, None)
+        if s == 0 and not args.no_order:
+            torch.cuda.synchronize()
+            cost = nev.view(C, nt).double().mean(0)
+            trip_order = torch.argsort(cost, descending=True)
+            order[0] = (torch.arange(C, device=dev).view(C, 1) * nt + trip_order.view(1, nt)).t().reshape(-1)
+            order[0] = order[0].to(torch.int32).contiguous()
     torch.cuda.synchronize()
     if dist:
         dist.barrier()
@@ -270,6 +279,7 @@ def run_ours(args):
                    "cosmologies_per_step": C, "triplets": nt, "rel_tol": 1e-4,
                    "l_range": "[1, 10/theta_min]" if lmax == 0 else f"[1, {lmax:g}]",
                    "l2": "flushed between steps (256 MB write)", "parallelism": f"replicas x{world}",
+                   "job_order": "none" if args.no_order else "longest-first by warm-up cost per triplet",
                    "max_rel_err_fp32_vs_fp64": max_rel, "fp64_check_integrals": int(v64.size),
                    "zero_valued_agree": zeros_agree},
         "e2e": {"value": e2e_val, "unit": "triplets/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
@@ -356,6 +366,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--region-cap", type=int, default=32768)
     ap.add_argument("--dump-costs", default="")
+    ap.add_argument("--no-order", action="store_true")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
     res = run_reference(args) if args.impl == "reference" else run_ours(args)

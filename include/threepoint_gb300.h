@@ -146,11 +146,15 @@ int tp_map3_batch(tp_ctx* ctx, const int* cosmo_index, int n_cosmo, const double
  * the context stream (no host synchronisation). job_cosmo/job_theta are
  * [n_jobs] and [n_jobs][3] device arrays; out/err are [n_jobs]; neval, nlive
  * and status are [n_jobs] (each may be NULL). nlive counts the cubature points
- * whose filter product is non-zero, i.e. whose line-of-sight sum was evaluated. */
+ * whose filter product is non-zero, i.e. whose line-of-sight sum was evaluated.
+ * job_order (optional, [n_jobs] device permutation) is the order in which the
+ * persistent grid takes the jobs: putting the most expensive integrals first
+ * shortens the tail of the launch (tp_map3_batch does this itself from the
+ * costs it has seen). Results are always written at the job's own index. */
 int tp_map3_jobs_device(tp_ctx* ctx, const int* job_cosmo_device, const double* job_theta_device, int n_jobs,
                         double phi_min, double phi_max, double l_min, double l_max, double rel_tol, int precision,
                         double* out_device, double* err_device, int64_t* neval_device, int64_t* nlive_device,
-                        int* status_device);
+                        int* status_device, const int* job_order_device);
 
 /* Replaces gamma0..gamma3(x1, x2, x3, z_max) (cuda_version/gamma.cu:98-148;
  * gamma.cuh:56-97): natural components of the shear 3PCF for n triangles

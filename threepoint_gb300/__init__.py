@@ -96,7 +96,7 @@ def lib():
         L.tp_bkappa_batch.argtypes = [p, ip, dp, l, i, dp]
         L.tp_pell_batch.argtypes = [p, i, dp, l, i, dp]
         L.tp_map3_batch.argtypes = [p, ip, i, dp, i, d, d, d, d, d, i, dp, dp, i64p, ip]
-        L.tp_map3_jobs_device.argtypes = [p, p, p, i, d, d, d, d, d, i, p, p, p, p, p]
+        L.tp_map3_jobs_device.argtypes = [p, p, p, i, d, d, d, d, d, i, p, p, p, p, p, p]
         L.tp_ctx_set_limits.argtypes = [p, i, i]
         L.tp_ctx_stream.restype = p
         L.tp_ctx_stream.argtypes = [p]
@@ -276,14 +276,15 @@ class Context:
         return float(self.map3_batch([thetas], [cosmo_index], phiMin, phiMax, lMin, precision=precision)[0, 0])
 
     def map3_jobs_device(self, job_cosmo, job_theta, out, err=None, neval=None, status=None, phiMin=0.0,
-                         phiMax=2 * math.pi, lMin=1.0, lMax=0.0, rel_tol=1e-4, precision=FP32, nlive=None):
+                         phiMax=2 * math.pi, lMin=1.0, lMax=0.0, rel_tol=1e-4, precision=FP32, nlive=None,
+                         job_order=None):
         """Asynchronous device-resident variant: arguments are torch CUDA
         tensors (int32 [n], float64 [n,3], float64 [n] ...)."""
         n = int(job_cosmo.numel())
         ptr = lambda t: C.c_void_p(t.data_ptr()) if t is not None else None
         _check(self._h, lib().tp_map3_jobs_device(self._h, ptr(job_cosmo), ptr(job_theta), n, phiMin, phiMax, lMin,
                                                   lMax, rel_tol, precision, ptr(out), ptr(err), ptr(neval),
-                                                  ptr(nlive), ptr(status)))
+                                                  ptr(nlive), ptr(status), ptr(job_order)))
 
     @property
     def stream_handle(self):

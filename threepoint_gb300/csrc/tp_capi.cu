@@ -458,7 +458,7 @@ extern "C" int tp_ctx_set_limits(tp_ctx* ctx, int region_cap, int max_ctas) {
 extern "C" int tp_map3_jobs_device(tp_ctx* ctx, const int* job_cosmo, const double* job_theta, int n_jobs,
                                    double phi_min, double phi_max, double l_min, double l_max, double rel_tol,
                                    int precision, double* out, double* err, int64_t* neval, int64_t* nlive,
-                                   int* status) {
+                                   int* status, const int* job_order) {
   if (!ctx || !job_cosmo || !job_theta || !out || n_jobs < 0) return TP_ERR_ARG;
   if (precision != TP_FP64 && precision != TP_FP32) return TP_ERR_ARG;
   if (!(rel_tol > 0) || !(phi_max > phi_min) || !(l_min >= 0)) return TP_ERR_ARG;
@@ -496,6 +496,7 @@ extern "C" int tp_map3_jobs_device(tp_ctx* ctx, const int* job_cosmo, const doub
   L.status = status;
   L.job_counter = ctx->d_counter;
   L.diag = ctx->d_diag;
+  L.job_order = job_order;
   e = launch_map3(L, grid, smem, ctx->d_scratch, ctx->stream);
   return tp_cuda(ctx, e, "map3 launch");
 }
@@ -521,32 +522,56 @@ extern "C" int tp_map3_batch(tp_ctx* ctx, const int* cosmo_index, int n_cosmo, c
       jc[j] = cidx[c];
       for (int q = 0; q < 3; ++q) jt[3 * (size_t)j + q] = thetas[3 * t + q];
     }
+  // longest-first order from the costs seen for the same triplets before
+  // (unseen triplets first); costs barely depend on the cosmology
+  std::vector<std::string> keys(n_trip);
+  std::vector<double> pred(n_trip);
+  for (int t = 0; t < n_trip; ++t) {
+    char buf[128];
+    snprintf(buf, sizeof(buf), "%a,%a,%a,%a,%a,%a,%a,%a,%d", thetas[3 * t], thetas[3 * t + 1], thetas[3 * t + 2],
+             phi_min, phi_max, l_min, l_max, rel_tol, precision);
+    keys[t] = buf;
+    auto it = ctx->map3_cost.find(keys[t]);
+    pred[t] = it == ctx->map3_cost.end() ? 1e300 : it->second;
+  }
+  std::vector<int> order(nj);
+  for (int j = 0; j < nj; ++j) order[j] = j;
+  std::stable_sort(order.begin(), order.end(),
+                   [&](int a, int b) { return pred[a % n_trip] > pred[b % n_trip]; });
   cudaSetDevice(ctx->device);
   size_t o_th = 0, o_c = (sizeof(double) * 3 * nj + 255) & ~size_t(255);
   size_t o_out = o_c + ((sizeof(int) * nj + 255) & ~size_t(255));
   size_t o_err = o_out + ((sizeof(double) * nj + 255) & ~size_t(255));
   size_t o_nev = o_err + ((sizeof(double) * nj + 255) & ~size_t(255));
   size_t o_st = o_nev + ((sizeof(int64_t) * nj + 255) & ~size_t(255));
-  size_t total = o_st + sizeof(int) * nj + 256;
+  size_t o_ord = o_st + ((sizeof(int) * nj + 255) & ~size_t(255));
+  size_t total = o_ord + sizeof(int) * nj + 256;
   int st = ctx->ensure_io(total);
   if (st) return st;
   char* b = ctx->d_io;
   cudaStream_t s = ctx->stream;
   cudaError_t e = cudaMemcpyAsync(b + o_th, jt.data(), sizeof(double) * 3 * nj, cudaMemcpyHostToDevice, s);
   if (e == cudaSuccess) e = cudaMemcpyAsync(b + o_c, jc.data(), sizeof(int) * nj, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(b + o_ord, order.data(), sizeof(int) * nj, cudaMemcpyHostToDevice, s);
   if (e != cudaSuccess) return tp_cuda(ctx, e, "map3 upload");
   st = tp_map3_jobs_device(ctx, (int*)(b + o_c), (double*)(b + o_th), nj, phi_min, phi_max, l_min, l_max, rel_tol,
                            precision, (double*)(b + o_out), (double*)(b + o_err), (int64_t*)(b + o_nev), nullptr,
-                           (int*)(b + o_st));
+                           (int*)(b + o_st), (int*)(b + o_ord));
   if (st) return st;
   std::vector<int> hst(nj);
+  std::vector<int64_t> hnev(nj);
   e = cudaMemcpyAsync(out, b + o_out, sizeof(double) * nj, cudaMemcpyDeviceToHost, s);
   if (e == cudaSuccess && err) e = cudaMemcpyAsync(err, b + o_err, sizeof(double) * nj, cudaMemcpyDeviceToHost, s);
-  if (e == cudaSuccess && neval)
-    e = cudaMemcpyAsync(neval, b + o_nev, sizeof(int64_t) * nj, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(hnev.data(), b + o_nev, sizeof(int64_t) * nj, cudaMemcpyDeviceToHost, s);
   if (e == cudaSuccess) e = cudaMemcpyAsync(hst.data(), b + o_st, sizeof(int) * nj, cudaMemcpyDeviceToHost, s);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);
   if (e != cudaSuccess) return tp_cuda(ctx, e, "map3");
+  if (neval) memcpy(neval, hnev.data(), sizeof(int64_t) * nj);
+  for (int t = 0; t < n_trip; ++t) {
+    double m = 0;
+    for (int c = 0; c < n_cosmo; ++c) m += (double)hnev[c * n_trip + t];
+    ctx->map3_cost[keys[t]] = m / n_cosmo;
+  }
   int bad = 0;
   for (int j = 0; j < nj; ++j) {
     if (status_out) status_out[j] = hst[j];

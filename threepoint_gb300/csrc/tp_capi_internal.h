@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 
 #include <string>
+#include <unordered_map>
 #include <vector>
 
 #include "tp_internal.cuh"
@@ -42,6 +43,9 @@ struct tp_ctx {
   size_t scratch_bytes = 0;
   char* d_io = nullptr;
   size_t io_bytes = 0;
+  // expected cost (cubature points) of each <Map^3> integral seen so far,
+  // keyed by triplet and settings; orders later launches longest-first
+  std::unordered_map<std::string, double> map3_cost;
   int* d_counter = nullptr;
   unsigned* d_diag = nullptr;
 

@@ -99,6 +99,7 @@ struct PellProd {
     int valid, los;
   };
   static constexpr int REC = (int)sizeof(Rec);
+  const int* job_order = nullptr;
   static constexpr size_t PSMEM = sizeof(R) * HC_COUNT * NNODE + sizeof(CosmoK<R>) + 64;
 
   const CovJob* jobs;
@@ -253,6 +254,7 @@ struct BkProd {
     int valid;
   };
   static constexpr int REC = (int)sizeof(Rec);
+  const int* job_order = nullptr;
   static constexpr size_t PSMEM = sizeof(R) * NCP * NNODE + sizeof(CosmoK<R>) + 64;
 
   const CovJob* jobs;

@@ -360,10 +360,14 @@ __device__ void adaptive_body(P& pol, int njobs, int* job_counter, const EngineC
   const int tid = threadIdx.x;
 
   for (;;) {
-    if (tid == 0) es->job = atomicAdd(job_counter, 1);
+    if (tid == 0) {
+      int k = atomicAdd(job_counter, 1);
+      es->job = (k < njobs && pol.job_order) ? pol.job_order[k] : k;
+      es->ktot = k;
+    }
     __syncthreads();
     const int job = es->job;
-    if (job >= njobs) break;
+    if (es->ktot >= njobs) break;
     double xmin[DIM], xmax[DIM];
     pol.begin_job(job, psmem, xmin, xmax);
     if (tid == 0) {

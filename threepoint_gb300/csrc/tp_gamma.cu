@@ -116,6 +116,7 @@ struct GammaPolicy {
     int live;
   };
   static constexpr int REC = (int)sizeof(Rec);
+  const int* job_order = nullptr;
   static constexpr int PD = 2;
   static constexpr int NS = 1;
   __device__ static int slot(int) { return 0; }

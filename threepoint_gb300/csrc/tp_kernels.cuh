@@ -68,6 +68,7 @@ struct Map3Launch {
   int64_t* neval;
   int64_t* nlive;
   int* status;
+  const int* job_order;  // optional device permutation of the job indices
   int* job_counter;  // device int
   unsigned* diag;    // device counter of bulk-copy timeouts (may be null)
 };

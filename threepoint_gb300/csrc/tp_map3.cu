@@ -12,6 +12,8 @@
 // shared memory with a bulk async copy when the CTA switches cosmology.
 #include <cuda_runtime.h>
 
+#include <type_traits>
+
 #include "tp_bispec.cuh"
 #include "tp_cubature.cuh"
 #include "tp_internal.cuh"
@@ -24,11 +26,22 @@ struct Map3Policy {
   static constexpr int G = 8;              // node groups per point
   static constexpr int NPG = NNODE / G;    // nodes per group
   static constexpr int CH = 8;             // regions per evaluation chunk
-  struct Rec {
-    Tri<R> tri;
-    double outer;  // l1 l2 uHat uHat uHat * node-weight scale
+  // Point records are read by consecutive threads for consecutive points, so
+  // the FP32 record has an odd number of 32-bit words (15): conflict-free
+  // shared-memory banks. FP32 keeps the filter product as its log2.
+  struct RecF {
+    Tri<float> tri;
+    float lo;  // log2(l1 l2 uHat uHat uHat)
+    int live;
+    float pad;
+  };
+  struct RecD {
+    Tri<double> tri;
+    double outer;  // l1 l2 uHat uHat uHat
     int live;
   };
+  typedef typename std::conditional<sizeof(R) == 4, RecF, RecD>::type Rec;
+  const int* job_order;
   static constexpr int REC = (int)sizeof(Rec);
   static constexpr int PD = 1;
   static constexpr int NS = 1;
@@ -141,17 +154,15 @@ struct Map3Policy {
       live = l1 > 1.0e-10f && l2 > 1.0e-10f && l3 > 1.0e-10f && t1 > 0.f && t2 > 0.f && t3 > 0.f;
       float L = M::lg2(l1 * l2) + M::lg2(t1) + M::lg2(t2) + M::lg2(t3) - LOG2E * (t1 + t2 + t3);
       live = live && L > -1070.f;
-      double outer = 0.0;
-      if (live) outer = (L > -120.f) ? (double)M::ex2(L) : exp2((double)L);
-      r.outer = outer * scale;
-      if (live) make_tri_phi_f(l1, l2, cphi, l3, *(Tri<float>*)&r.tri);
+      r.lo = L;
+      if (live) make_tri_phi_f(l1, l2, cphi, l3, r.tri);
     } else {
       double l1 = x[0], l2 = x[1], phi = x[2];
       double s = l1 * l1 + l2 * l2 + 2 * l1 * l2 * cos(phi);
       double l3 = s > 0 ? sqrt(s) : 0.0;
       double outer = l1 * l2 * uhat(l1 * th[0]) * uhat(l2 * th[1]) * uhat(l3 * th[2]);
       live = !(l1 == 0 || l2 == 0 || l3 == 0) && l1 > 1.0e-10 && l2 > 1.0e-10 && l3 > 1.0e-10 && outer != 0.0;
-      r.outer = outer * scale;
+      r.outer = outer;
       if (live) make_tri<R>(l1, l2, l3, r.tri);
     }
     r.live = live;
@@ -178,7 +189,16 @@ struct Map3Policy {
 
   __device__ void finalize(const char* recp, const double* sum, double* fv) {
     const Rec& r = *(const Rec*)recp;
-    fv[0] = r.live ? r.outer * sum[0] : 0.0;
+    if (!r.live) {
+      fv[0] = 0.0;
+      return;
+    }
+    double outer;
+    if constexpr (sizeof(R) == 4)
+      outer = (r.lo > -120.f) ? (double)Mth<float>::ex2(r.lo) : exp2((double)r.lo);
+    else
+      outer = r.outer;
+    fv[0] = outer * scale * sum[0];
   }
 
   __device__ void end_job(int job, const double* V, const double* E, long long nev, int st) {
@@ -297,6 +317,7 @@ static cudaError_t launch_map3_t(const Map3Launch& L, int grid, size_t smem, cha
   pol.nlive = L.nlive;
   pol.status = L.status;
   pol.diag = L.diag;
+  pol.job_order = L.job_order;
   EngineCfg cfg{0.0, L.rel_tol, TP_NORM_L1, L.cap, L.max_sweeps};
   size_t slot = Slot<3, 1>::bytes(L.cap);
   k_map3<R, MAP3_NT><<<grid, MAP3_NT, smem, st>>>(pol, L.njobs, L.job_counter, cfg, scratch, slot);
