@@ -156,6 +156,23 @@ int tp_map3_jobs_device(tp_ctx* ctx, const int* job_cosmo_device, const double* 
                         double* out_device, double* err_device, int64_t* neval_device, int64_t* nlive_device,
                         int* status_device, const int* job_order_device);
 
+/* Allocation-free variant of tp_map3_jobs_device; no counterpart in the
+ * reference. For callers that cannot allocate device memory when they
+ * integrate (inside CUDA stream capture, under a framework-owned allocator,
+ * in pipelines that forbid allocation after start-up): it calls no cudaMalloc
+ * or cudaFree and keeps the per-CTA region stores in a fixed 128 MiB
+ * __device__ array of the library (held on every GPU that loads the library
+ * until exit). Limits: at most 8192 regions per integral (an integral that
+ * needs more stops with status != 0 and TP_ERR_CAPACITY is reported through
+ * status_device) and a grid trimmed to fit the array. The first call on a
+ * device looks up the array's device address (cudaGetSymbolAddress): make it
+ * before any stream capture. All calls share the array, so calls that overlap
+ * on the GPU race; serialise them. Inputs, outputs and the context's
+ * cosmology tables are the caller's/the context's, as in tp_map3_jobs_device. */
+int tp_map3_jobs_noalloc(tp_ctx* ctx, const int* job_cosmo_device, const double* job_theta_device, int n_jobs,
+                         double phi_min, double phi_max, double l_min, double l_max, double rel_tol, int precision,
+                         double* out_device, double* err_device, int* status_device);
+
 /* Replaces gamma0..gamma3(x1, x2, x3, z_max) (cuda_version/gamma.cu:98-148;
  * gamma.cuh:56-97): natural components of the shear 3PCF for n triangles
  * x[3i..3i+2] (radians) of one cosmology, by Ogata Hankel quadrature

@@ -98,6 +98,7 @@ def lib():
         L.tp_map3_batch.argtypes = [p, ip, i, dp, i, d, d, d, d, d, i, dp, dp, i64p, ip]
         L.tp_map3_jobs_device.argtypes = [p, p, p, i, d, d, d, d, d, i, p, p, p, p, p, p]
         L.tp_ctx_set_limits.argtypes = [p, i, i]
+        L.tp_map3_jobs_noalloc.argtypes = [p, p, p, i, d, d, d, d, d, i, p, p, p]
         L.tp_ctx_stream.restype = p
         L.tp_ctx_stream.argtypes = [p]
         L.tp_pipe_peaks.argtypes = [i, dp]
