@@ -44,8 +44,9 @@ enum {
 /* error norm of a vector integrand (cubature.h) */
 enum { TP_NORM_INDIVIDUAL = 0, TP_NORM_PAIRED, TP_NORM_L2, TP_NORM_L1, TP_NORM_LINF };
 
-/* survey geometry of the covariance (calculateApertureStatisticsCovariance.cu:111-130) */
-enum { TP_GEOM_CIRCLE = 0, TP_GEOM_SQUARE = 1, TP_GEOM_INFINITE = 2 };
+/* survey geometry of the covariance (calculateApertureStatisticsCovariance.cu:111-130);
+ * the rectangle's second side is set by tp_set_rectangle_side */
+enum { TP_GEOM_CIRCLE = 0, TP_GEOM_SQUARE = 1, TP_GEOM_INFINITE = 2, TP_GEOM_RECTANGLE = 3 };
 
 /* Cosmological parameters; same fields and meaning as the reference's class
  * cosmology (cuda_version/cosmology.cuh:13-29). */
@@ -81,6 +82,39 @@ int tp_read_thetas(const char* path, double* out, int cap, int* n_out);
 /* convert_angle_to_rad (cuda_version/helpers.cu:130-153); unit "arcmin", "deg" or "rad" */
 int tp_convert_angle_to_rad(double value, const char* unit, double* out);
 
+/* Survey parameters of the covariance; same fields as the reference's class
+ * covarianceParameters (cuda_version/cosmology.cuh:44-56), angles in rad,
+ * density in rad^-2, area in rad^2. */
+typedef struct {
+  double theta_max, theta_max_smaller, shapenoise_sigma, galaxy_density, area;
+  int shapenoise_only;
+} tp_cov_params;
+
+/* Replaces covarianceParameters::covarianceParameters(fn) (cuda_version/cosmology.cu:92-170):
+ * "name value" lines (thetaMax, thetaMax_smaller, shapenoise_sigma,
+ * galaxy_density, unit, shapenoiseOnly, area), '#' comments; converts to rad
+ * with the file's unit. Unlike the reference, an unknown name or unit is an
+ * error (TP_ERR_FORMAT) instead of a message and half-converted values. */
+int tp_cov_params_from_file(const char* path, tp_cov_params* out);
+
+/* (r, u, v) binning of the shear 3PCF; the reference's struct configGamma
+ * (cuda_version/helpers.cuh:48-52), r in arcmin. */
+typedef struct {
+  int rsteps, usteps, vsteps;
+  double umin, umax, vmin, vmax, rmin, rmax;
+} tp_gamma_config;
+
+/* Replaces read_gamma_config (cuda_version/helpers.cu:242-318): "name value"
+ * lines rmin, rmax, umin, umax, vmin, vmax, rsteps, usteps, vsteps. An unknown
+ * name is TP_ERR_FORMAT (the reference prints a message and stops reading). */
+int tp_gamma_config_from_file(const char* path, tp_gamma_config* out);
+
+/* Triangles of the bin centres of calculateGamma (cuda_version/calculateGamma.cu:104-121),
+ * r-major, then u, then v: r log-spaced, u and v linear; r2 = r [arcmin -> rad],
+ * r3 = u r2, r1 = v r3 + r2. x_out[3i..3i+2] = (r1, r2, r3) [rad],
+ * ruv_out[3i..3i+2] = (r [arcmin], u, v); ruv_out may be NULL. */
+int tp_gamma_triangles(const tp_gamma_config* cfg, double* x_out, double* ruv_out);
+
 /* ---- context ------------------------------------------------------------ */
 int tp_ctx_create(int device, tp_ctx** out);
 int tp_ctx_destroy(tp_ctx* ctx);
@@ -113,6 +147,11 @@ int tp_set_cosmologies(tp_ctx* ctx, const tp_cosmology* cosmo, int n_cosmo, cons
  * covariance (globals sigma, n, constant_powerspectrum of the reference:
  * bispectrum.cu:21-23, initCovariance apertureStatisticsCovariance.cu:30-45). */
 int tp_set_shape_noise(tp_ctx* ctx, double sigma_eps, double n_gal_per_rad2, int constant_powerspectrum);
+
+/* Smaller side [rad] of a rectangular survey (TP_GEOM_RECTANGLE), the global
+ * thetaMax_smaller of the reference (apertureStatisticsCovariance.cu:24,154-172):
+ * the window is sinc^2(lx*theta_max/2) * sinc^2(ly*theta_max_smaller/2). */
+int tp_set_rectangle_side(tp_ctx* ctx, double theta_max_smaller);
 
 /* Copies cosmology i's FP64 tables to the host: 6*256 doubles
  * (f_K, g, D1, r_sigma, n_eff, ncur) followed by norm. */
@@ -197,8 +236,9 @@ int tp_cov_total_batch(tp_ctx* ctx, int cosmo_index, int term, int geometry, dou
 
 /* Single covariance terms T1(th1..th6), T2(th1..th6), T4(th1..th6)
  * (apertureStatisticsCovariance.cu:1065-1197) for n six-tuples th6[n][6],
- * without the permutation sums. T2 is 0 for the infinite geometry; T4 is
- * evaluated in the infinite geometry normalised by area. *n_capped (optional)
+ * without the permutation sums. T2 is 0 for the infinite geometry; T4 exists
+ * only for the infinite geometry (normalised by area), as in the reference,
+ * whose T4 throws for the others (TP_ERR_ARG here). *n_capped (optional)
  * receives the number of integrals that hit a cap. */
 int tp_cov_term_batch(tp_ctx* ctx, int cosmo_index, int term, int geometry, double theta_max, double area,
                       const double* th6, int n, int precision, double* out, int* n_capped);

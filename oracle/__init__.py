@@ -31,7 +31,8 @@ class Cosmo(C.Structure):
 
 
 class CovParams(C.Structure):
-    _fields_ = [("type", C.c_int), ("thetaMax", C.c_double), ("area", C.c_double), ("lMin", C.c_double)]
+    _fields_ = [("type", C.c_int), ("thetaMax", C.c_double), ("area", C.c_double), ("lMin", C.c_double),
+                ("thetaMaxSmaller", C.c_double)]
 
 
 INTEGRAND_V = C.CFUNCTYPE(C.c_int, C.c_uint, C.c_size_t, C.POINTER(C.c_double), C.c_void_p, C.c_uint,

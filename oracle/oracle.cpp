@@ -1264,14 +1264,18 @@ extern "C" void orc_ggg_analytic(double r1, double r2, double r3, double* re, do
 // ===========================================================================
 namespace {
 
-// window of a square survey, apertureStatisticsCovariance.cu:132-153
-double G_square(double thetaMax, double lx, double ly) {
-  double t1 = 0.5 * lx * thetaMax, t2 = 0.5 * ly * thetaMax;
+// window of a square survey, apertureStatisticsCovariance.cu:132-153, and of
+// a rectangle with sides thetaMax (x) and thetaMaxY (y), :154-172
+double G_rect(double thetaMax, double thetaMaxY, double lx, double ly) {
+  double t1 = 0.5 * lx * thetaMax, t2 = 0.5 * ly * thetaMaxY;
   double j1 = fabs(t1) <= 1e-6 ? 1 : sin(t1) / t1;
   double j2 = fabs(t2) <= 1e-6 ? 1 : sin(t2) / t2;
   return j1 * j1 * j2 * j2;
 }
 // circular window, apertureStatisticsCovariance.cu:117-130
+double G_square(double thetaMax, double lx, double ly) { return G_rect(thetaMax, thetaMax, lx, ly); }
+// second side of the window: thetaMax except for the rectangle
+double side_y(const orc_cov_params* p) { return p->type == 3 ? p->thetaMaxSmaller : p->thetaMax; }
 double G_circle(double thetaMax, double ell) {
   double tmp = thetaMax * ell;
   double r = std::cyl_bessel_j(1.0, tmp);
@@ -1312,8 +1316,8 @@ int integrand_T1_v(unsigned ndim, size_t npts, const double* x, void* fdata, uns
       double ell3 = sqrt(e * e + f * f);
       bool zero;
       double G;
-      if (c->p->type == 1) {
-        G = G_square(c->p->thetaMax, a, b);
+      if (c->p->type == 1 || c->p->type == 3) {
+        G = G_rect(c->p->thetaMax, side_y(c->p), a, b);
         zero = ell1 <= 0 || ell2 <= 0 || ell3 <= 0 || ell3 > c->lMax;
       } else {
         G = G_circle(c->p->thetaMax, sqrt(a * a + b * b));
@@ -1346,9 +1350,9 @@ int integrand_T2_v(unsigned ndim, size_t npts, const double* x, void* fdata, uns
     if (c->part == 1) {
       double ell = x[i * ndim];
       if (!(ell < c->p->lMin)) res = ell * Pell(c->t, ell) * uHat(ell * c->th1) * uHat(ell * c->th2);
-    } else if (c->p->type == 1) {
+    } else if (c->p->type == 1 || c->p->type == 3) {
       double lx = x[i * ndim], ly = x[i * ndim + 1];
-      double G = G_square(c->p->thetaMax, lx, ly);
+      double G = G_rect(c->p->thetaMax, side_y(c->p), lx, ly);
       double ell = sqrt(lx * lx + ly * ly);
       // ell = 0 (the centre of the symmetric box) is the integrand's limit 0;
       // the reference evaluates Pell(0) there, which is NaN

@@ -91,10 +91,11 @@ void orc_ggg_analytic(double r1, double r2, double r3, double* re, double* im);
 
 // ---- <Map^3> covariance (cuda_version/apertureStatisticsCovariance.cu) ----
 typedef struct {
-  int type;          // 0 circle, 1 square, 2 infinite (3 rectangular unsupported)
+  int type;          // 0 circle, 1 square, 2 infinite, 3 rectangular
   double thetaMax;   // rad
   double area;       // rad^2
   double lMin;       // integration lower bound used by T1 (infinite) and T2
+  double thetaMaxSmaller;  // rad, second side of the rectangle (type 3)
 } orc_cov_params;
 double orc_T1(const orc_tables* t, const orc_cov_params* p, const double* th6, double relTol, long* neval);
 double orc_T2(const orc_tables* t, const orc_cov_params* p, const double* th6);

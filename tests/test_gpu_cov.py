@@ -91,6 +91,32 @@ def test_t1_square_shapenoise_matches_oracle(shapenoise_ctx, shapenoise_oracle):
     assert got == pytest.approx(ref, rel=1e-6)
 
 
+@pytest.mark.parametrize("term", [1, 2])
+def test_rectangle_matches_oracle(shapenoise_ctx, shapenoise_oracle, term):
+    """Rectangular survey (G_rectangle, sides thetaMax and thetaMax_smaller)."""
+    import threepoint_gb300 as tp
+
+    small = 0.4 * TMAX
+    shapenoise_ctx.set_rectangle_side(small)
+    got = shapenoise_ctx.cov_term(term, TH6, geometry=tp.GEOM_RECTANGLE, thetaMax=TMAX, area=AREA, precision=0)[0]
+    ref = shapenoise_oracle.cov_T(term, O.CovParams(3, TMAX, AREA, 0.0, small), TH6)[0]
+    assert got == pytest.approx(ref, rel=1e-5 if term == 1 else 1e-6)
+    # a rectangle with equal sides is the square
+    shapenoise_ctx.set_rectangle_side(TMAX)
+    sq = shapenoise_ctx.cov_term(term, TH6, geometry=tp.GEOM_SQUARE, thetaMax=TMAX, area=AREA, precision=0)[0]
+    re = shapenoise_ctx.cov_term(term, TH6, geometry=tp.GEOM_RECTANGLE, thetaMax=TMAX, area=AREA, precision=0)[0]
+    assert re == sq
+
+
+def test_t4_only_infinite(cov_ctx):
+    """The reference's T4 throws for finite geometries; here TP_ERR_ARG."""
+    import threepoint_gb300 as tp
+
+    for geom in (tp.GEOM_CIRCLE, tp.GEOM_SQUARE, tp.GEOM_RECTANGLE):
+        with pytest.raises(tp.ThreepointError):
+            cov_ctx.cov_term(4, TH6, geometry=geom, thetaMax=TMAX, area=AREA)
+
+
 @pytest.mark.parametrize("term,geom", [(1, 2), (2, 1), (1, 1)])
 def test_totals_match_oracle(shapenoise_ctx, shapenoise_oracle, term, geom):
     """The permutation tables of T1_total/T2_total against the oracle's, over

@@ -24,7 +24,7 @@ LIB_PATH = os.path.join(HERE, "build", "libthreepoint_gb300.so")
 
 TP_OK, TP_ERR_ARG, TP_ERR_IO, TP_ERR_FORMAT, TP_ERR_CUDA, TP_ERR_STATE, TP_ERR_CAPACITY, TP_ERR_NOMEM = range(8)
 FP64, FP32 = 0, 1
-GEOM_CIRCLE, GEOM_SQUARE, GEOM_INFINITE = 0, 1, 2
+GEOM_CIRCLE, GEOM_SQUARE, GEOM_INFINITE, GEOM_RECTANGLE = 0, 1, 2, 3
 N_REDSHIFT_BINS = 256
 ARCMIN = 2.9088820866e-4
 
@@ -64,6 +64,66 @@ class cosmology:
 
     def _c(self):
         return _Cosmo(**{f.name: float(getattr(self, f.name)) for f in fields(self)})
+
+
+class _CovParams(C.Structure):
+    _fields_ = [(n, C.c_double) for n in ("theta_max", "theta_max_smaller", "shapenoise_sigma", "galaxy_density",
+                                           "area")] + [("shapenoise_only", C.c_int)]
+
+
+@dataclass
+class covarianceParameters:
+    """Survey parameters of the covariance (cuda_version/cosmology.cuh:44-56);
+    angles in rad, galaxy density in rad^-2, area in rad^2."""
+    theta_max: float = 0.0
+    theta_max_smaller: float = 0.0
+    shapenoise_sigma: float = 0.0
+    galaxy_density: float = 1.0
+    area: float = 0.0
+    shapenoise_only: bool = False
+
+    @classmethod
+    def from_file(cls, path):
+        """cuda_version/cosmology.cu:92-170"""
+        c = _CovParams()
+        _check(None, lib().tp_cov_params_from_file(str(path).encode(), C.byref(c)))
+        return cls(c.theta_max, c.theta_max_smaller, c.shapenoise_sigma, c.galaxy_density, c.area,
+                   bool(c.shapenoise_only))
+
+
+class _GammaConfig(C.Structure):
+    _fields_ = [(n, C.c_int) for n in ("rsteps", "usteps", "vsteps")] + [
+        (n, C.c_double) for n in ("umin", "umax", "vmin", "vmax", "rmin", "rmax")]
+
+
+@dataclass
+class configGamma:
+    """(r, u, v) binning of the shear 3PCF (cuda_version/helpers.cuh:48-52), r in arcmin."""
+    rsteps: int = 10
+    usteps: int = 10
+    vsteps: int = 10
+    umin: float = 0.0
+    umax: float = 1.0
+    vmin: float = -1.0
+    vmax: float = 1.0
+    rmin: float = 0.1
+    rmax: float = 100.0
+
+    @classmethod
+    def from_file(cls, path):
+        """read_gamma_config (cuda_version/helpers.cu:242-318)"""
+        c = _GammaConfig()
+        _check(None, lib().tp_gamma_config_from_file(str(path).encode(), C.byref(c)))
+        return cls(**{f.name: getattr(c, f.name) for f in fields(cls)})
+
+    def triangles(self):
+        """Bin-centre triangles of calculateGamma (calculateGamma.cu:104-121):
+        returns x [n,3] (r1, r2, r3) in rad and ruv [n,3] (r [arcmin], u, v)."""
+        c = _GammaConfig(**{f.name: getattr(self, f.name) for f in fields(self)})
+        n = self.rsteps * self.usteps * self.vsteps
+        x, ruv = np.zeros(3 * n), np.zeros(3 * n)
+        _check(None, lib().tp_gamma_triangles(C.byref(c), _dp(x), _dp(ruv)))
+        return x.reshape(n, 3), ruv.reshape(n, 3)
 
 
 _lib = None
@@ -106,6 +166,10 @@ def lib():
         L.tp_ogata_weights.argtypes = [dp]
         L.tp_cov_total_batch.argtypes = [p, i, i, i, d, d, dp, dp, i, i, dp, ip]
         L.tp_cov_term_batch.argtypes = [p, i, i, i, d, d, dp, i, i, dp, ip]
+        L.tp_set_rectangle_side.argtypes = [p, d]
+        L.tp_cov_params_from_file.argtypes = [C.c_char_p, C.POINTER(_CovParams)]
+        L.tp_gamma_config_from_file.argtypes = [C.c_char_p, C.POINTER(_GammaConfig)]
+        L.tp_gamma_triangles.argtypes = [C.POINTER(_GammaConfig), dp, dp]
         _lib = L
     return _lib
 
@@ -223,6 +287,10 @@ class Context:
 
     def set_shape_noise(self, sigma_eps, n_gal_per_rad2, constant_powerspectrum=False):
         _check(self._h, lib().tp_set_shape_noise(self._h, sigma_eps, n_gal_per_rad2, int(constant_powerspectrum)))
+
+    def set_rectangle_side(self, theta_max_smaller):
+        """Second side [rad] of a rectangular survey (GEOM_RECTANGLE)."""
+        _check(self._h, lib().tp_set_rectangle_side(self._h, theta_max_smaller))
 
     def tables(self, i=0):
         out = np.zeros(6 * 256 + 1)

@@ -20,8 +20,14 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-I" + os.path.join(ROOT, "include")]
 
 
+CLI = os.path.join(HERE, "cli")
+BIN = os.path.join(BUILD, "bin")
+# command-line drivers, named like the reference's executables
+CLIS = ("calculateApertureStatistics", "calculateGamma", "calculateApertureStatisticsCovariance")
+
+
 def sources():
-    return sorted(f for f in os.listdir(CSRC) if f.endswith(".cu"))
+    return sorted(f for f in os.listdir(CSRC) if f.endswith((".cu", ".cpp")))
 
 
 def _nvcc():
@@ -36,21 +42,29 @@ def _nvcc():
 
 def _deps_mtime():
     m = 0.0
-    for d in (CSRC, os.path.join(ROOT, "include")):
+    for d in (CSRC, CLI, os.path.join(ROOT, "include")):
         for f in os.listdir(d):
             m = max(m, os.path.getmtime(os.path.join(d, f)))
     return m
 
 
+def _cli_cmds():
+    cxx = os.environ.get("CXX", "g++")
+    return [[cxx, "-O2", "-std=c++17", "-I" + os.path.join(ROOT, "include"), os.path.join(CLI, c + ".cpp"),
+             "-L" + BUILD, "-lthreepoint_gb300", "-Wl,-rpath,$ORIGIN/..", "-o", os.path.join(BIN, c + ".x")]
+            for c in CLIS]
+
+
 def build(force: bool = False, verbose: bool = False, extra=()) -> str:
-    os.makedirs(BUILD, exist_ok=True)
-    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= _deps_mtime():
+    os.makedirs(BIN, exist_ok=True)
+    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= _deps_mtime() and all(
+            os.path.exists(os.path.join(BIN, c + ".x")) for c in CLIS):
         return LIB
     nvcc = _nvcc()
     objs = []
     cmds = []
     for s in sources():
-        o = os.path.join(BUILD, s[:-3] + ".o")
+        o = os.path.join(BUILD, os.path.splitext(s)[0] + ".o")
         objs.append(o)
         cmds.append([nvcc, *ARCH, *FLAGS, *extra, "-c", os.path.join(CSRC, s), "-o", o])
 
@@ -68,7 +82,18 @@ def build(force: bool = False, verbose: bool = False, extra=()) -> str:
     r = subprocess.run(link, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("link failed:\n" + r.stdout + r.stderr)
+    with cf.ThreadPoolExecutor(max_workers=len(CLIS)) as ex:
+        for cmd, r in ex.map(run, _cli_cmds()):
+            if verbose or r.returncode != 0:
+                sys.stderr.write(" ".join(cmd) + "\n" + r.stdout + r.stderr)
+            if r.returncode != 0:
+                raise RuntimeError("driver build failed: " + cmd[-1])
     return LIB
+
+
+def driver(name: str) -> str:
+    """Path of a built command-line driver (calculateGamma etc.)."""
+    return os.path.join(BIN, name + ".x")
 
 
 if __name__ == "__main__":

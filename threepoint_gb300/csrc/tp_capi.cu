@@ -111,6 +111,83 @@ extern "C" int tp_cosmology_from_file(const char* path, tp_cosmology* out) {
   return TP_OK;
 }
 
+extern "C" int tp_cov_params_from_file(const char* path, tp_cov_params* out) {
+  if (!path || !out) return TP_ERR_ARG;
+  std::vector<std::pair<std::string, std::string>> kv;
+  if (!read_name_value_lines(path, kv)) return TP_ERR_IO;
+  tp_cov_params c;
+  memset(&c, 0, sizeof(c));
+  std::string unit;
+  for (auto& p : kv) {
+    const char* v = p.second.c_str();
+    if (p.first == "thetaMax") c.theta_max = atof(v);
+    else if (p.first == "thetaMax_smaller") c.theta_max_smaller = atof(v);
+    else if (p.first == "shapenoise_sigma") c.shapenoise_sigma = atof(v);
+    else if (p.first == "galaxy_density") c.galaxy_density = atof(v);
+    else if (p.first == "unit") unit = p.second;
+    else if (p.first == "shapenoiseOnly") c.shapenoise_only = atoi(v) != 0;
+    else if (p.first == "area") c.area = atof(v);
+    else return TP_ERR_FORMAT;
+  }
+  // unit conversion as at the end of the reference constructor (cosmology.cu:162-169)
+  double one;
+  if (tp_convert_angle_to_rad(1.0, unit.c_str(), &one)) return TP_ERR_FORMAT;
+  c.theta_max *= one;
+  c.theta_max_smaller *= one;
+  c.area = c.area * one * one;
+  c.galaxy_density = c.galaxy_density / one / one;
+  *out = c;
+  return TP_OK;
+}
+
+extern "C" int tp_gamma_config_from_file(const char* path, tp_gamma_config* out) {
+  if (!path || !out) return TP_ERR_ARG;
+  std::vector<std::pair<std::string, std::string>> kv;
+  if (!read_name_value_lines(path, kv)) return TP_ERR_IO;
+  tp_gamma_config c;
+  memset(&c, 0, sizeof(c));
+  int seen = 0;
+  for (auto& p : kv) {
+    const double v = atof(p.second.c_str());
+    if (p.first == "rmin") c.rmin = v, seen |= 1;
+    else if (p.first == "rmax") c.rmax = v, seen |= 2;
+    else if (p.first == "umin") c.umin = v, seen |= 4;
+    else if (p.first == "umax") c.umax = v, seen |= 8;
+    else if (p.first == "vmin") c.vmin = v, seen |= 16;
+    else if (p.first == "vmax") c.vmax = v, seen |= 32;
+    else if (p.first == "rsteps") c.rsteps = (int)std::round(v), seen |= 64;
+    else if (p.first == "usteps") c.usteps = (int)std::round(v), seen |= 128;
+    else if (p.first == "vsteps") c.vsteps = (int)std::round(v), seen |= 256;
+    else return TP_ERR_FORMAT;
+  }
+  if (seen != 511) return TP_ERR_FORMAT;
+  *out = c;
+  return TP_OK;
+}
+
+extern "C" int tp_gamma_triangles(const tp_gamma_config* cfg, double* x, double* ruv) {
+  if (!cfg || !x || cfg->rsteps < 1 || cfg->usteps < 1 || cfg->vsteps < 1 || !(cfg->rmin > 0) || !(cfg->rmax > 0))
+    return TP_ERR_ARG;
+  const double lrmin = log(cfg->rmin), lrmax = log(cfg->rmax);
+  long t = 0;
+  for (int i = 0; i < cfg->rsteps; i++) {
+    const double r = exp(lrmin + (lrmax - lrmin) / cfg->rsteps * (i + 0.5));
+    for (int j = 0; j < cfg->usteps; j++) {
+      const double u = cfg->umin + (cfg->umax - cfg->umin) / cfg->usteps * (j + 0.5);
+      for (int k = 0; k < cfg->vsteps; k++, t++) {
+        const double v = cfg->vmin + (cfg->vmax - cfg->vmin) / cfg->vsteps * (k + 0.5);
+        const double r2 = r * M_PI / 180. / 60.;  // Jarvis et al. (2004) binning
+        const double r3 = r2 * u;
+        x[3 * t] = v * r3 + r2;
+        x[3 * t + 1] = r2;
+        x[3 * t + 2] = r3;
+        if (ruv) ruv[3 * t] = r, ruv[3 * t + 1] = u, ruv[3 * t + 2] = v;
+      }
+    }
+  }
+  return TP_OK;
+}
+
 extern "C" int tp_rebin_n_of_z(const double* zs, const double* ns, int nf, int n_bins, double zmax, double* nz_out) {
   if (!zs || !ns || !nz_out || nf < 2 || n_bins <= 0 || !(zmax > 0)) return TP_ERR_ARG;
   const double zmin_f = zs[0], zmax_f = zs[nf - 1];
@@ -387,6 +464,12 @@ extern "C" int tp_set_shape_noise(tp_ctx* ctx, double sigma_eps, double n_gal, i
   ctx->sigma_eps = sigma_eps;
   ctx->ngal = n_gal;
   ctx->constant_ps = constant_ps != 0;
+  return TP_OK;
+}
+
+extern "C" int tp_set_rectangle_side(tp_ctx* ctx, double theta_max_smaller) {
+  if (!ctx || !(theta_max_smaller > 0)) return TP_ERR_ARG;
+  ctx->theta_max_smaller = theta_max_smaller;
   return TP_OK;
 }
 

@@ -37,6 +37,8 @@ struct tp_ctx {
   // shape noise of P(ell)
   double sigma_eps = 0.0, ngal = 1.0;
   int constant_ps = 0;
+  // second side of a rectangular survey [rad]; 0 = not set
+  double theta_max_smaller = 0.0;
 
   // scratch: per-CTA region stores; io: staging of host-API inputs/outputs
   char* d_scratch = nullptr;

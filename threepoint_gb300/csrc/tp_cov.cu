@@ -61,9 +61,11 @@ __device__ __forceinline__ R pell_node(const R* __restrict__ hc, int j, R ell, R
 }
 
 // windows of the survey geometries (apertureStatisticsCovariance.cu:117-153)
+// G_square is the rectangle with two equal sides; G_rectangle (:154-172) has
+// side thetaMax along lx and thetaMax_smaller along ly
 template <typename R>
-__device__ inline R g_square(R thetaMax, R lx, R ly) {
-  R t1 = (R)0.5 * lx * thetaMax, t2 = (R)0.5 * ly * thetaMax;
+__device__ inline R g_square(R thetaMax, R thetaMaxY, R lx, R ly) {
+  R t1 = (R)0.5 * lx * thetaMax, t2 = (R)0.5 * ly * thetaMaxY;
   R j1 = fabs(t1) <= (R)1e-6 ? (R)1 : sin(t1) / t1;
   R j2 = fabs(t2) <= (R)1e-6 ? (R)1 : sin(t2) / t2;
   return j1 * j1 * j2 * j2;
@@ -107,7 +109,7 @@ struct PellProd {
   CosmoK<R> ck;
   double psn;      // shape-noise power 0.5 sigma^2 / n
   int constant_ps;
-  double thetaMax;
+  double thetaMax, thetaMaxY;  // survey sides (equal unless rectangular)
   double norm;     // final normalisation of each integral
   double* out;
   int* status;
@@ -160,7 +162,7 @@ struct PellProd {
       ell[2] = sqrt(e * e + f * f);
       double G;
       if constexpr (KIND == K_T1_SQUARE) {
-        G = (double)g_square<R>((R)thetaMax, (R)a, (R)b);
+        G = (double)g_square<R>((R)thetaMax, (R)thetaMaxY, (R)a, (R)b);
         zero = ell[0] <= 0 || ell[1] <= 0 || ell[2] <= 0 || ell[2] > lmax;
       } else {
         G = (double)g_circle<R>((R)thetaMax, (R)sqrt(a * a + b * b));
@@ -188,7 +190,7 @@ struct PellProd {
       // ell = 0 (the box centre) is the integrand's limit 0; the reference
       // evaluates Pell(0) there, which is NaN
       zero = ell[0] < lmin || ell[0] == 0;
-      if (!zero) wt = uhat(ell[0] * th[0]) * uhat(ell[0] * th[1]) * (double)g_square<R>((R)thetaMax, (R)lx, (R)ly);
+      if (!zero) wt = uhat(ell[0] * th[0]) * uhat(ell[0] * th[1]) * (double)g_square<R>((R)thetaMax, (R)thetaMaxY, (R)lx, (R)ly);
     } else {
       ell[0] = x[0];
       zero = ell[0] < lmin || ell[0] == 0;
@@ -509,8 +511,8 @@ struct JobSet {
 };
 
 template <typename R, int DIM, int KIND>
-static int run_pell_kind(tp_ctx* ctx, int cosmo, const JobSet& js, double theta_max, double norm, double rel_tol,
-                         std::vector<double>& res, int& bad) {
+static int run_pell_kind(tp_ctx* ctx, int cosmo, const JobSet& js, double theta_max, double theta_max_y,
+                         double norm, double rel_tol, std::vector<double>& res, int& bad) {
   res.assign(js.jobs.size(), 0.0);
   if (js.jobs.empty()) return TP_OK;
   const size_t n = js.jobs.size();
@@ -535,6 +537,7 @@ static int run_pell_kind(tp_ctx* ctx, int cosmo, const JobSet& js, double theta_
   pol.psn = 0.5 * ctx->sigma_eps * ctx->sigma_eps / ctx->ngal;
   pol.constant_ps = ctx->constant_ps;
   pol.thetaMax = theta_max;
+  pol.thetaMaxY = theta_max_y;
   pol.norm = norm;
   pol.out = (double*)(b + o_o);
   pol.status = (int*)(b + o_s);
@@ -596,6 +599,9 @@ static int cov_terms(tp_ctx* ctx, int cosmo, int term, int geom, double theta_ma
   const size_t n = th6.size();
   out.assign(n, 0.0);
   const double two_pi = 2 * PI;
+  // the rectangle runs the square kinds with its second side
+  const bool boxy = geom == TP_GEOM_SQUARE || geom == TP_GEOM_RECTANGLE;
+  const double tmy = geom == TP_GEOM_RECTANGLE ? ctx->theta_max_smaller : theta_max;
   if (term == 1) {
     JobSet js;
     std::vector<int> id(n);
@@ -608,11 +614,11 @@ static int cov_terms(tp_ctx* ctx, int cosmo, int term, int geom, double theta_ma
     int st;
     if (geom == TP_GEOM_INFINITE) {
       if (!(area > 0)) return tp_fail(ctx, TP_ERR_ARG, "T1 (infinite) needs area > 0");
-      st = run_pell_kind<R, 3, K_T1_INF>(ctx, cosmo, js, theta_max, 2 / area / pow(two_pi, 3), 1e-4, r, bad);
-    } else if (geom == TP_GEOM_SQUARE) {
-      st = run_pell_kind<R, 6, K_T1_SQUARE>(ctx, cosmo, js, theta_max, 1 / pow(two_pi, 6), 1e-2, r, bad);
+      st = run_pell_kind<R, 3, K_T1_INF>(ctx, cosmo, js, theta_max, tmy, 2 / area / pow(two_pi, 3), 1e-4, r, bad);
+    } else if (boxy) {
+      st = run_pell_kind<R, 6, K_T1_SQUARE>(ctx, cosmo, js, theta_max, tmy, 1 / pow(two_pi, 6), 1e-2, r, bad);
     } else {
-      st = run_pell_kind<R, 6, K_T1_CIRCLE>(ctx, cosmo, js, theta_max, 1 / pow(two_pi, 6), 1e-2, r, bad);
+      st = run_pell_kind<R, 6, K_T1_CIRCLE>(ctx, cosmo, js, theta_max, tmy, 1 / pow(two_pi, 6), 1e-2, r, bad);
     }
     if (st) return st;
     for (size_t i = 0; i < n; ++i) out[i] = r[id[i]];
@@ -630,18 +636,18 @@ static int cov_terms(tp_ctx* ctx, int cosmo, int term, int geom, double theta_ma
       double a12[2] = {t[0], t[1]}, a56[2] = {t[4], t[5]}, b34[2] = {t[2], t[3]};
       i1[i] = ja.add(a12, 2, 0.0, l1);
       i2[i] = ja.add(a56, 2, 0.0, l1);
-      if (geom == TP_GEOM_SQUARE)
+      if (boxy)
         i3[i] = jb.add(b34, 2, 0.0, 10. / std::min(t[2], t[3]));
       else
         i3[i] = jb.add(b34, 2, 0.0, l1);
     }
     std::vector<double> ra, rb;
-    int st = run_pell_kind<R, 1, K_T2_A>(ctx, cosmo, ja, theta_max, 1 / two_pi, 1e-4, ra, bad);
+    int st = run_pell_kind<R, 1, K_T2_A>(ctx, cosmo, ja, theta_max, tmy, 1 / two_pi, 1e-4, ra, bad);
     if (st) return st;
-    if (geom == TP_GEOM_SQUARE)
-      st = run_pell_kind<R, 2, K_T2_B_SQUARE>(ctx, cosmo, jb, theta_max, 1 / (two_pi * two_pi), 1e-4, rb, bad);
+    if (boxy)
+      st = run_pell_kind<R, 2, K_T2_B_SQUARE>(ctx, cosmo, jb, theta_max, tmy, 1 / (two_pi * two_pi), 1e-4, rb, bad);
     else
-      st = run_pell_kind<R, 1, K_T2_B_CIRCLE>(ctx, cosmo, jb, theta_max, 1 / two_pi, 1e-4, rb, bad);
+      st = run_pell_kind<R, 1, K_T2_B_CIRCLE>(ctx, cosmo, jb, theta_max, tmy, 1 / two_pi, 1e-4, rb, bad);
     if (st) return st;
     for (size_t i = 0; i < n; ++i) out[i] = ra[i1[i]] * ra[i2[i]] * rb[i3[i]];
     return TP_OK;
@@ -695,9 +701,12 @@ static int check_cov_args(tp_ctx* ctx, int cosmo, int term, int geom, int precis
   if (!ctx) return TP_ERR_ARG;
   if (cosmo < 0 || cosmo >= ctx->n_cosmo) return tp_fail(ctx, TP_ERR_STATE, "no such cosmology");
   if (term != 1 && term != 2 && term != 4) return tp_fail(ctx, TP_ERR_ARG, "term must be 1, 2 or 4");
-  if (geom < TP_GEOM_CIRCLE || geom > TP_GEOM_INFINITE) return tp_fail(ctx, TP_ERR_ARG, "unknown geometry");
-  if (term == 4 && geom != TP_GEOM_INFINITE && geom != TP_GEOM_SQUARE)
-    return tp_fail(ctx, TP_ERR_ARG, "T4 is defined for the infinite geometry (with the survey area)");
+  if (geom < TP_GEOM_CIRCLE || geom > TP_GEOM_RECTANGLE) return tp_fail(ctx, TP_ERR_ARG, "unknown geometry");
+  // the reference's T4 throws for every geometry but the infinite one (apertureStatisticsCovariance.cu:1183-1195)
+  if (term == 4 && geom != TP_GEOM_INFINITE)
+    return tp_fail(ctx, TP_ERR_ARG, "T4: only coded for the infinite survey geometry");
+  if (geom == TP_GEOM_RECTANGLE && !(ctx->theta_max_smaller > 0))
+    return tp_fail(ctx, TP_ERR_STATE, "rectangular geometry needs tp_set_rectangle_side");
   if (precision != TP_FP64 && precision != TP_FP32) return TP_ERR_ARG;
   return TP_OK;
 }
