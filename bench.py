@@ -137,6 +137,7 @@ def run_ours(args):
     import torch
 
     import threepoint_gb300 as tp
+    from threepoint_gb300.shard import shard_range
 
     rank, world, local = dist_env()
     torch.cuda.set_device(local)
@@ -166,9 +167,13 @@ def run_ours(args):
     lmax = 0.0 if args.lmax == "ref" else float(args.lmax)
     flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=dev)  # > 129 MB L2
 
+    # each rank walks through its own contiguous block of the LHS (weak scaling,
+    # no communication on the data path)
+    lo, hi = shard_range(N_LHS, rank, world)
+
     def cosmo_batch(step):
-        off = ((rank * (args.steps + args.warmup) + step) * C) % (N_LHS - C)
-        return [tp.cosmology(**c) for c in cosmos_all[off:off + C]]
+        off = lo + (step * C) % max(1, hi - lo - C + 1)
+        return [tp.cosmology(**c) for c in (cosmos_all * 2)[off:off + C]]
 
     order = [None]
 
@@ -239,6 +244,22 @@ def run_ours(args):
     max_rel = float(np.max(np.abs(v32[nz_mask] - v64[nz_mask]) / np.abs(v64[nz_mask])))
     zeros_agree = bool(np.array_equal(v32 == 0, v64 == 0))
 
+    # plain FP64 GPU method on the same workload shape (2 cosmologies x 220),
+    # device-resident like `value`; outside the timed region
+    c64 = 2
+    n64 = c64 * nt
+    fp64_val = None
+    if not args.no_fp64_plain:
+        ctx.set_cosmologies(cosmo_batch(args.warmup)[:c64], nz)
+        e64 = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+        with torch.cuda.stream(stream):
+            e64[0].record(stream)
+            ctx.map3_jobs_device(job_cosmo[:n64], job_theta[:n64], out[:n64], err[:n64], nev[:n64], status[:n64],
+                                 lMax=lmax, rel_tol=1e-4, precision=tp.FP64)
+            e64[1].record(stream)
+        torch.cuda.synchronize()
+        fp64_val = n64 / (e64[0].elapsed_time(e64[1]) * 1e-3)
+
     # e2e: the public host API (host inputs, host outputs) for the same steps
     e2e_steps = max(1, min(args.steps, 3))
     torch.cuda.synchronize()
@@ -283,13 +304,16 @@ def run_ours(args):
                    "max_rel_err_fp32_vs_fp64": max_rel, "fp64_check_integrals": int(v64.size),
                    "zero_valued_agree": zeros_agree},
         "e2e": {"value": e2e_val, "unit": "triplets/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
-        "gpu_launches": 7 * args.steps,
+        "gpu_launches": 8 * args.steps,  # 7 table-build kernels + k_map3 per step
         "roofline": {"bound": "sfu", "achieved": achieved / 1e9, "peak": sfu_peak / 1e9, "unit": "Gop/s",
                      "frac": achieved / sfu_peak, "traffic": None,
                      "peak_source": "measured now by tp_pipe_peaks (ex2.approx.f32 loop, whole device)",
                      "kernel": "k_map3<float>", "kernel_ms_per_launch": map3_avg_s * 1e3,
                      "fp32_fma_peak_tflops": f32_peak / 1e12, "fp64_fma_peak_tflops": f64_peak / 1e12},
         "clocks": clocks,
+        "plain_fp64_gpu": None if fp64_val is None else {
+            "value": fp64_val, "unit": "triplets/s", "integrals": n64, "fp32_speedup": value / fp64_val,
+            "note": "same kernel with the FP64 BiHalofit integrand, integrals only"},
         "wall_s": wall,
     }
     if not args.no_cpu_baseline:
@@ -367,6 +391,7 @@ def main():
     ap.add_argument("--region-cap", type=int, default=32768)
     ap.add_argument("--dump-costs", default="")
     ap.add_argument("--no-order", action="store_true")
+    ap.add_argument("--no-fp64-plain", action="store_true", help="skip the plain FP64 comparison run")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
     res = run_reference(args) if args.impl == "reference" else run_ours(args)

@@ -260,6 +260,104 @@ __device__ __forceinline__ R bispec_node(const R* __restrict__ nc, int j, const 
   }
 }
 
+// ---------------------------------------------------------------------------
+// FP32 point path of <Map^3> and b_kappa: NF_* node rows (tp_internal.cuh).
+// Per triangle it keeps ell_i^2 besides the Tri fields; the record is 15 words.
+struct TriF {
+  float l[3], lg[3], l2[3];
+  float log2r1, r2sq, pr2;
+  float f2t[3];
+};
+
+__device__ __forceinline__ void trif_from_tri(const Tri<float>& T, TriF& F) {
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    F.l[i] = T.l[i];
+    F.lg[i] = T.lg[i];
+    F.l2[i] = T.l[i] * T.l[i];
+    F.f2t[i] = T.f2t[i];
+  }
+  F.log2r1 = T.log2r1;
+  F.r2sq = T.r2sq;
+  F.pr2 = T.pr2;
+}
+
+// P_lin(ell h / f_K) from the node's row: the cubic log2 P table when present
+// (table coordinate lg * (N-1)/(HI-LO) + NF_TOFF; the integer part by a
+// round-down add of 1.5 * 2^23, no float/int conversions), else plin().
+__device__ __forceinline__ float plin_fast(const CosmoK<float>& K, const float* __restrict__ c, float l, float lg) {
+  typedef Mth<float> M;
+  if (K.plt) {
+    constexpr float INV = (float)((PLT_N - 1) / (PLT_HI - PLT_LO));
+    float t = fmaf(lg, INV, c[NF_TOFF]);
+    t = fminf(fmaxf(t, 0.f), (float)(PLT_N - 1) - 1e-3f);
+    const float tm = __fadd_rd(t, 12582912.f);  // 1.5 * 2^23 + floor(t)
+    const int i = __float_as_int(tm) - 0x4B400000;
+    const float f = t - (tm - 12582912.f);
+    const float4 q = reinterpret_cast<const float4*>(K.plt)[i];
+    return M::ex2(fmaf(f, fmaf(f, fmaf(f, q.w, q.z), q.y), q.x));
+  }
+  return plin<float>(K, l * c[NF_HF], lg + c[NF_L2HF]);
+}
+
+// B at one node from its NF_* row (the bispec_eval formula, B4-B9 of
+// Takahashi et al. 2020, with the folded coefficients); W not applied.
+__device__ __forceinline__ float bispec_fast(const float* __restrict__ c, const TriF& T, const CosmoK<float>& K) {
+  typedef Mth<float> M;
+  float lq[3], P[3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i) lq[i] = T.lg[i] + c[NF_L2S];
+  if (c[NF_TREE] != 0.f) {
+#pragma unroll
+    for (int i = 0; i < 3; ++i) P[i] = plin_fast(K, c, T.l[i], T.lg[i]);
+    return c[NF_D1P4] * 2.f * (T.f2t[0] * P[0] * P[1] + T.f2t[1] * P[1] * P[2] + T.f2t[2] * P[2] * P[0]);
+  }
+  // 1-halo term: 1 / ((a_n q^al + b_n q^be) (1 + 1/(c_n q))) per side
+  const float l2an = c[NF_ANA] - M::ex2(fmaf(c[NF_ANC], T.log2r1, c[NF_L2ANR]));
+  const float al = fminf(M::ex2(fmaf(c[NF_ALD], T.r2sq, c[NF_ALA])), K.alpha_max);
+  const float be = c[NF_BETAB] * T.pr2;
+  float bs1h = 1.f;
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    const float cq = c[NF_CNS] * T.l[i];
+    const float den = M::ex2(fmaf(al, lq[i], l2an)) + M::ex2(fmaf(be, lq[i], c[NF_L2BN]));
+    bs1h *= cq * M::rcp(den * (cq + 1.f));
+  }
+  // 3-halo term
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    const float num = fmaf(c[NF_D1SQFNS2], T.l2[i], c[NF_D1SQ]);
+    const float den = fmaf(c[NF_HNS2], T.l2[i], fmaf(c[NF_GNS], T.l[i], 1.f));
+    const float a = num * M::rcp(den) * plin_fast(K, c, T.l[i], T.lg[i]);
+    const float x = c[NF_PNS] * T.l[i];
+    const float x3 = x * x * x;
+    const float mq = M::ex2(fmaf(c[NF_MUN], lq[i], c[NF_L2MN])) + M::ex2(fmaf(c[NF_NUN], lq[i], c[NF_L2NN]));
+    P[i] = fmaf(x3, M::rcp(mq * (x3 + 1.f)), a);
+  }
+  const float dn = c[NF_DNS], en = c[NF_ENS];
+  float bs3h = fmaf(dn, T.l[2], T.f2t[0]) * P[0] * P[1];
+  bs3h = fmaf(fmaf(dn, T.l[0], T.f2t[1]) * P[1], P[2], bs3h);
+  bs3h = fmaf(fmaf(dn, T.l[1], T.f2t[2]) * P[2], P[0], bs3h);
+  const float e3 = fmaf(en, T.l[0], 1.f) * fmaf(en, T.l[1], 1.f) * fmaf(en, T.l[2], 1.f);
+  return fmaf(2.f * bs3h, M::rcp(e3), bs1h);
+}
+
+// W B at node j of an NF_* table (node-major, 16-byte rows)
+__device__ __forceinline__ float bispec_node_fast(const float* __restrict__ nf, int j, const TriF& T,
+                                                  const CosmoK<float>& K) {
+  float c[NCP];
+  const float4* v = reinterpret_cast<const float4*>(nf + j * NCP);
+#pragma unroll
+  for (int q = 0; q < NCP / 4; ++q) {
+    float4 t = v[q];
+    c[4 * q] = t.x;
+    c[4 * q + 1] = t.y;
+    c[4 * q + 2] = t.z;
+    c[4 * q + 3] = t.w;
+  }
+  return c[NF_W] * bispec_fast(c, T, K);
+}
+
 // Mid-bin two-point interpolation of a z table at fractional bin position fb
 // (cuda_version/bispectrum.cu:335-437) with the lower neighbour clamped at bin 0.
 __host__ __device__ inline void interp_mid_w(double fb, int& i0, int& i1, double& w0, double& w1) {

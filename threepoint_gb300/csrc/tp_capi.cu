@@ -289,6 +289,7 @@ void tp_ctx::free_cosmo() {
   cudaFree(d_nz);
   cudaFree(d_ncoef64);
   cudaFree(d_ncoef32);
+  cudaFree(d_fcoef32);
   cudaFree(d_hcoef);
   cudaFree(d_hcoef32);
   cudaFree(d_wscale64);
@@ -302,6 +303,7 @@ void tp_ctx::free_cosmo() {
   d_nz = nullptr;
   d_ncoef64 = nullptr;
   d_ncoef32 = nullptr;
+  d_fcoef32 = nullptr;
   d_hcoef = nullptr;
   d_hcoef32 = nullptr;
   d_wscale64 = d_wscale32 = nullptr;
@@ -427,6 +429,7 @@ extern "C" int tp_set_cosmologies(tp_ctx* ctx, const tp_cosmology* cosmo, int n,
     if (e == cudaSuccess) e = dalloc(&ctx->d_nz, (size_t)cap * NZ);
     if (e == cudaSuccess) e = dalloc(&ctx->d_ncoef64, (size_t)cap * NCP * NNODE);
     if (e == cudaSuccess) e = dalloc(&ctx->d_ncoef32, (size_t)cap * NCP * NNODE);
+    if (e == cudaSuccess) e = dalloc(&ctx->d_fcoef32, (size_t)cap * NCP * NNODE);
     if (e == cudaSuccess) e = dalloc(&ctx->d_hcoef, (size_t)cap * HC_COUNT * NNODE);
     if (e == cudaSuccess) e = dalloc(&ctx->d_hcoef32, (size_t)cap * HC_COUNT * NNODE);
     if (e == cudaSuccess) e = dalloc(&ctx->d_wscale64, cap);
@@ -452,7 +455,7 @@ extern "C" int tp_set_cosmologies(tp_ctx* ctx, const tp_cosmology* cosmo, int n,
       e = cudaMemcpyAsync((char*)ctx->d_tab + (size_t)i * sizeof(TablesDev) + offsetof(TablesDev, pk), pk + (size_t)i * NK, sizeof(double) * NK, cudaMemcpyHostToDevice, s);
   if (e == cudaSuccess)
     e = build_tables(ctx->d_cos, ctx->d_eh, ctx->d_nz, nz_stride, ctx->d_tab, ctx->d_ncoef64, ctx->d_ncoef32,
-                     ctx->d_hcoef, ctx->d_hcoef32, ctx->d_wscale64, ctx->d_wscale32, (CosmoK<double>*)ctx->d_ck64,
+                     ctx->d_fcoef32, ctx->d_hcoef, ctx->d_hcoef32, ctx->d_wscale64, ctx->d_wscale32, (CosmoK<double>*)ctx->d_ck64,
                      (CosmoK<float>*)ctx->d_ck32, ctx->d_plt, n, s);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);
   if (e != cudaSuccess) return tp_cuda(ctx, e, "table build");
@@ -518,7 +521,7 @@ extern "C" int tp_bkappa_batch(tp_ctx* ctx, const int* cosmo_index, const double
   if (e == cudaSuccess && cosmo_index) e = cudaMemcpyAsync(base + off_idx, cosmo_index, b_idx, cudaMemcpyHostToDevice, s);
   if (e == cudaSuccess)
     e = launch_bkappa_points(precision, cosmo_index ? (int*)(base + off_idx) : nullptr, (double*)base, n,
-                             precision == TP_FP64 ? (const void*)ctx->d_ncoef64 : (const void*)ctx->d_ncoef32,
+                             precision == TP_FP64 ? (const void*)ctx->d_ncoef64 : (const void*)ctx->d_fcoef32,
                              precision == TP_FP64 ? ctx->d_wscale64 : ctx->d_wscale32,
                              precision == TP_FP64 ? ctx->d_ck64 : ctx->d_ck32, (double*)(base + off_out), s);
   if (e == cudaSuccess) e = cudaMemcpyAsync(out, base + off_out, b_out, cudaMemcpyDeviceToHost, s);
@@ -561,6 +564,7 @@ extern "C" int tp_map3_jobs_device(tp_ctx* ctx, const int* job_cosmo, const doub
   L.job_theta = job_theta;
   L.ncoef64 = ctx->d_ncoef64;
   L.ncoef32 = ctx->d_ncoef32;
+  L.fcoef32 = ctx->d_fcoef32;
   L.wscale64 = ctx->d_wscale64;
   L.wscale32 = ctx->d_wscale32;
   L.ck64 = ctx->d_ck64;

@@ -26,6 +26,7 @@ struct tp_ctx {
   double* d_nz = nullptr;
   double* d_ncoef64 = nullptr;
   float* d_ncoef32 = nullptr;
+  float* d_fcoef32 = nullptr;  // NF_* rows of the FP32 point path
   double* d_hcoef = nullptr;
   float* d_hcoef32 = nullptr;
   double* d_wscale64 = nullptr;

@@ -74,6 +74,39 @@ enum NodeCoef {
 constexpr int NCP = 28;
 static_assert(NC_COUNT <= NCP, "node coefficient pitch");
 
+// FP32 node rows of the <Map^3> / b_kappa point path: the same BiHalofit
+// coefficients with every product that does not involve the triangle folded
+// in (q_i = ell_i s enters only through s-scaled coefficients; multiplicative
+// factors of powers are added to their log2 exponents), so that one
+// (point, node) evaluation needs fewer instructions. Same pitch and node-major
+// layout as the NC_* rows.
+enum FastCoef {
+  NF_W = 0,     // NC_W / wscale
+  NF_L2S,       // log2(s), s = r_sigma / f_K        (log2 q_i = lg_i + NF_L2S)
+  NF_L2HF,      // log2(h / f_K)
+  NF_HF,        // h / f_K
+  NF_TOFF,      // (NF_L2HF - PLT_LO) * (PLT_N-1)/(PLT_HI-PLT_LO): P_lin table coordinate offset
+  NF_ANA,       // log2 a_n = NF_ANA - ex2(NF_ANC log2 r1 + NF_L2ANR)
+  NF_L2ANR,     // log2(0.310 log2(10))
+  NF_ANC,
+  NF_L2BN,      // log2 b_n
+  NF_CNS,       // c_n s
+  NF_ALA, NF_ALD, NF_BETAB,
+  NF_D1SQ,      // D1^2
+  NF_D1SQFNS2,  // D1^2 f_n s^2
+  NF_GNS,       // g_n s
+  NF_HNS2,      // h_n s^2
+  NF_L2MN, NF_L2NN,  // log2 m_n, log2 n_n
+  NF_MUN, NF_NUN,
+  NF_PNS,       // p_n s
+  NF_ENS,       // e_n s
+  NF_DNS,       // d_n s
+  NF_TREE,      // 1 when z > 10
+  NF_D1P4,      // D1^4
+  NF_COUNT
+};
+static_assert(NF_COUNT <= NCP, "fast node coefficient pitch");
+
 // Per-node Halofit coefficients for the P_kappa line-of-sight integral
 // (P_k_nonlinear + limber prefactor at the fixed nodes; z-only parts).
 enum HaloCoef {

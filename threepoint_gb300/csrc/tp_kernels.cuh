@@ -57,6 +57,7 @@ struct Map3Launch {
   const double* job_theta;  // device [njobs][3]
   const double* ncoef64;    // device node coefficients (FP64, weight column normalised)
   const float* ncoef32;
+  const float* fcoef32;  // NF_* rows, read by the FP32 kernel
   const double* wscale64;   // device [n_cosmo] weight scales
   const double* wscale32;
   const void* ck64;         // device CosmoK<double>[n_cosmo]

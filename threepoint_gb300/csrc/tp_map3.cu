@@ -19,6 +19,18 @@
 #include "tp_internal.cuh"
 #include "tp_kernels.cuh"
 
+// Launch shape of the FP32 kernel: resident CTAs per SM requested from the
+// register allocator, and how many line-of-sight nodes one thread evaluates
+// per loop iteration (build-time tuning knobs, see threepoint_gb300/build.py).
+#ifndef TP_MAP3_MINB
+#define TP_MAP3_MINB 3
+#endif
+#ifndef TP_MAP3_UNROLL
+#define TP_MAP3_UNROLL 4
+#endif
+#define TP_PRAGMA(x) _Pragma(#x)
+#define TP_UNROLL(n) TP_PRAGMA(unroll n)
+
 namespace tp {
 
 template <typename R>
@@ -27,13 +39,12 @@ struct Map3Policy {
   static constexpr int NPG = NNODE / G;    // nodes per group
   static constexpr int CH = 8;             // regions per evaluation chunk
   // Point records are read by consecutive threads for consecutive points, so
-  // the FP32 record has an odd number of 32-bit words (15): conflict-free
+  // the FP32 record has an odd number of 32-bit words (17): conflict-free
   // shared-memory banks. FP32 keeps the filter product as its log2.
   struct RecF {
-    Tri<float> tri;
+    TriF tri;
     float lo;  // log2(l1 l2 uHat uHat uHat)
     int live;
-    float pad;
   };
   struct RecD {
     Tri<double> tri;
@@ -52,7 +63,7 @@ struct Map3Policy {
   // inputs
   const int* job_cosmo;
   const double* job_theta;
-  const R* node_coef;        // [n_cosmo][NC_COUNT][NNODE] (weights normalised, see wscale)
+  const R* node_coef;        // [n_cosmo][NNODE][NCP]: NC_* rows (FP64) or NF_* rows (FP32), weights / wscale
   const double* wscale;      // [n_cosmo]
   const CosmoK<R>* ck;       // [n_cosmo]
   double lmin, lmax, phimin, phimax;
@@ -155,7 +166,11 @@ struct Map3Policy {
       float L = M::lg2(l1 * l2) + M::lg2(t1) + M::lg2(t2) + M::lg2(t3) - LOG2E * (t1 + t2 + t3);
       live = live && L > -1070.f;
       r.lo = L;
-      if (live) make_tri_phi_f(l1, l2, cphi, l3, r.tri);
+      if (live) {
+        Tri<float> t;
+        make_tri_phi_f(l1, l2, cphi, l3, t);
+        trif_from_tri(t, r.tri);
+      }
     } else {
       double l1 = x[0], l2 = x[1], phi = x[2];
       double s = l1 * l1 + l2 * l2 + 2 * l1 * l2 * cos(phi);
@@ -176,9 +191,13 @@ struct Map3Policy {
     const CosmoK<R> K = *s_ck;
     KSum<R> acc;
     const int j0 = g * NPG;
-#pragma unroll 2
+    TP_UNROLL(TP_MAP3_UNROLL)
     for (int j = j0; j < j0 + NPG; ++j) {
-      R v = bispec_node<R>(s_nc, j, r.tri, K);
+      R v;
+      if constexpr (sizeof(R) == 4)
+        v = bispec_node_fast(s_nc, j, r.tri, K);
+      else
+        v = bispec_node<R>(s_nc, j, r.tri, K);
       if (v != v) v = (R)0;  // NaN in bispec -> 0 (bispectrum.cu:327-331)
       acc.add(v);
     }
@@ -214,7 +233,7 @@ struct Map3Policy {
 };
 
 template <typename R, int NT>
-__global__ void __launch_bounds__(NT, sizeof(R) == 4 ? 3 : 1) k_map3(Map3Policy<R> pol_in, int njobs, int* job_counter, EngineCfg cfg,
+__global__ void __launch_bounds__(NT, sizeof(R) == 4 ? TP_MAP3_MINB : 1) k_map3(Map3Policy<R> pol_in, int njobs, int* job_counter, EngineCfg cfg,
                                              char* scratch, size_t slot_bytes) {
   Map3Policy<R> pol = pol_in;
   pol.cur_cosmo = -1;
@@ -258,10 +277,20 @@ __global__ void k_bkappa_points(const int* cosmo_idx, const double* ell, long n,
   const R* nc = node_coef + (size_t)c * NCP * NNODE;
   const CosmoK<R> K = ck[c];
   KSum<R> acc;
-  for (int j = lane; j < NNODE; j += 32) {
-    R v = bispec_node<R>(nc, j, T, K);
-    if (v != v) v = (R)0;
-    acc.add(v);
+  if constexpr (sizeof(R) == 4) {
+    TriF F;
+    trif_from_tri(T, F);
+    for (int j = lane; j < NNODE; j += 32) {
+      float v = bispec_node_fast(nc, j, F, K);
+      if (v != v) v = 0.f;
+      acc.add(v);
+    }
+  } else {
+    for (int j = lane; j < NNODE; j += 32) {
+      R v = bispec_node<R>(nc, j, T, K);
+      if (v != v) v = (R)0;
+      acc.add(v);
+    }
   }
   double s = (double)acc.s;
   for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
@@ -304,7 +333,7 @@ static cudaError_t launch_map3_t(const Map3Launch& L, int grid, size_t smem, cha
   Map3Policy<R> pol;
   pol.job_cosmo = L.job_cosmo;
   pol.job_theta = L.job_theta;
-  pol.node_coef = (const R*)(sizeof(R) == 8 ? (const void*)L.ncoef64 : (const void*)L.ncoef32);
+  pol.node_coef = (const R*)(sizeof(R) == 8 ? (const void*)L.ncoef64 : (const void*)L.fcoef32);
   pol.wscale = sizeof(R) == 8 ? L.wscale64 : L.wscale32;
   pol.ck = (const CosmoK<R>*)(sizeof(R) == 8 ? L.ck64 : L.ck32);
   pol.lmin = L.lmin;

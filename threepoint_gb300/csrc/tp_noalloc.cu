@@ -92,6 +92,7 @@ extern "C" int tp_map3_jobs_noalloc(tp_ctx* ctx, const int* job_cosmo_device, co
   L.job_theta = job_theta_device;
   L.ncoef64 = ctx->d_ncoef64;
   L.ncoef32 = ctx->d_ncoef32;
+  L.fcoef32 = ctx->d_fcoef32;
   L.wscale64 = ctx->d_wscale64;
   L.wscale32 = ctx->d_wscale32;
   L.ck64 = ctx->d_ck64;

@@ -106,18 +106,58 @@ __device__ inline double d_window(double x, int i) {
   return (3 * (x * x - 3) * sin(x) + 9 * x * cos(x)) / x / x / x / x;
 }
 
-__device__ inline double sigma_integrand(const CosmoDev& c, const EHConst& e, const double* pk, double k, double r,
-                                         int j) {
-  double w = d_window(k * r, j);
-  return k * k * k * d_linear_pk(c, e, pk, k) * (j < 3 ? w * w : w);
+// Integrand in ln k of sigmam (bispectrum.cu:823-832): k^3 P(k) W(kr)^2 for
+// j < 3, k^3 P(k) W(kr) for j = 3, at k = exp(t). For the Gaussian windows
+// (j = 1..3) the powers k^3, (kh)^ns and exp(-(kr)^2) are folded into one exp;
+// the values agree with the literal form to rounding.
+__device__ inline double sigma_integrand(const CosmoDev& c, const EHConst& e, const double* pk, double k, double t,
+                                         double r, int j, double lnh, double lnkmin) {
+  if (j == 0) {
+    double w = d_window(k * r, 0);
+    return k * k * k * d_linear_pk(c, e, pk, k) * w * w;
+  }
+  const double x2 = (k * r) * (k * r);
+  double v;
+  if (c.pk_given) {
+    double p;
+    if (k >= c.kmax) {
+      p = pk[NK - 1];
+    } else if (k <= c.kmin) {
+      p = pk[0];
+    } else {
+      double didx = (t - lnkmin) / c.dk;
+      int idx = (int)didx;
+      didx -= idx;
+      p = idx >= NK - 1 ? pk[NK - 1] : pk[idx] * (1 - didx) + pk[idx + 1] * didx;
+    }
+    v = exp(3.0 * t - x2) * p;
+  } else {
+    // Eisenstein & Hu no-wiggle shape (bispectrum.cu:602-693) times k^3 W^2
+    const double kk = k * e.h;
+    const double xs = 0.43 * kk * e.sh;
+    const double xs2 = xs * xs;
+    const double geff = e.omh2 * (e.sa + e.one_m_sa / (1.0 + xs2 * xs2));
+    const double qeff = kk / geff * e.theta2;
+    const double L = log(2.718281828 + e.c184 * qeff);
+    const double C = 14.4 + 325.0 / (1.0 + 60.5 * exp(1.11 * log(qeff)));
+    const double rr = L / (L + C * qeff * qeff);
+    v = e.ehc * exp((3.0 + e.ns) * t + e.ns * lnh - x2) * rr * rr;
+  }
+  if (j == 1) return v;
+  if (j == 2) return v * x2;
+  return v * x2 * (1 - x2);
 }
 
 // sigma(R): nested doubling trapezoid in ln k (bispectrum.cu:796-852). All 32
 // lanes of the calling warp cooperate on the trapezoid sums and return the
-// same value (xor-butterfly sums are bitwise identical in every lane).
+// same value (xor-butterfly sums are bitwise identical in every lane). Each
+// doubling evaluates only the new odd points and adds them to the previous
+// level's sum: the even points of level n are bitwise the points of level n/2
+// (hh is halved exactly), so this is the reference's sum in another order.
 __device__ double warp_sigmam(const CosmoDev& c, const EHConst& e, const double* pk, double r, int j) {
   if (c.sigma8 < 1e-8) return 0;
   const int lane = threadIdx.x & 31;
+  const double lnh = log(e.h), lnkmin = c.pk_given ? log(c.kmin) : 0.0;
   double k1 = 2. * PI / r, k2 = 2. * PI / r;
   double xx = 0, xxpp = -1.0;
   // iteration caps: at most 2^22 trapezoid points per pass; a non-finite sum
@@ -128,14 +168,26 @@ __device__ double warp_sigmam(const CosmoDev& c, const EHConst& e, const double*
     double a = log(k1), b = log(k2);
     double xxp = -1.0;
     int n = 2;
-    double ends = 0.5 * (sigma_integrand(c, e, pk, k1, r, j) + sigma_integrand(c, e, pk, k2, r, j));
+    double ends = 0.5 * (sigma_integrand(c, e, pk, k1, a, r, j, lnh, lnkmin) + sigma_integrand(c, e, pk, k2, b, r, j, lnh, lnkmin));
+    double sum = 0;
     for (int inner = 0; inner < 21; ++inner) {
       n = n * 2;
       double hh = (b - a) / (double)n;
       double part = 0;
-      for (int i = 1 + lane; i < n; i += 32) part += sigma_integrand(c, e, pk, exp(a + hh * i), r, j);
+      if (n == 4) {  // first level: all three interior points
+        for (int i = 1 + lane; i < 4; i += 32) {
+          double t = a + hh * i;
+          part += sigma_integrand(c, e, pk, exp(t), t, r, j, lnh, lnkmin);
+        }
+      } else {
+        for (int m = lane; m < n / 2; m += 32) {
+          double t = a + hh * (2 * m + 1);
+          part += sigma_integrand(c, e, pk, exp(t), t, r, j, lnh, lnkmin);
+        }
+      }
       for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
-      xx = (part + ends) * hh;
+      sum += part;
+      xx = (sum + ends) * hh;
       if (!isfinite(xx) || fabs((xx - xxp) / xx) < EPS) break;
       xxp = xx;
     }
@@ -318,8 +370,8 @@ __device__ inline double interp_mid(const double* arr, double zfrac_bins) {
 // Per-node coefficients of b_kappa's LOS integral (z-only parts of
 // integrand_bkappa + bispec, bispectrum.cu:221-333) and of P_kappa's
 // (limber_integrand_power_spectrum + P_k_nonlinear, bispectrum.cu:531-600,951-991).
-__global__ void k_node_coefs(const CosmoDev* cos, const TablesDev* tab, double* ncoef, float* ncoef_f, double* hcoef,
-                             float* hcoef_f, int n) {
+__global__ void k_node_coefs(const CosmoDev* cos, const TablesDev* tab, double* ncoef, float* ncoef_f, float* fcoef_f,
+                             double* hcoef, float* hcoef_f, int n) {
   int ci = blockIdx.x;
   int j = threadIdx.x;
   if (ci >= n || j >= NNODE) return;
@@ -375,6 +427,37 @@ __global__ void k_node_coefs(const CosmoDev* cos, const TablesDev* tab, double* 
       o[q] = q < NC_COUNT ? v[q] : 0.0;
       of[q] = q < NC_COUNT ? (float)v[q] : 0.f;
     }
+    // folded FP32 row of the point path (NF_*); NF_W is normalised in k_finish
+    const double sq = rs / fK, hf = c.h / fK;
+    double f[NF_COUNT];
+    f[NF_W] = W;
+    f[NF_L2S] = log2(sq);
+    f[NF_L2HF] = log2(hf);
+    f[NF_HF] = hf;
+    f[NF_TOFF] = (log2(hf) - PLT_LO) * ((PLT_N - 1) / (PLT_HI - PLT_LO));
+    f[NF_ANA] = v[NC_ANA];
+    f[NF_L2ANR] = log2(v[NC_ANR]);
+    f[NF_ANC] = v[NC_ANC];
+    f[NF_L2BN] = LOG2_10 * (-3.428 - 2.681 * ls + 1.624 * ls * ls - 0.095 * ls * ls * ls);
+    f[NF_CNS] = v[NC_CN] * sq;
+    f[NF_ALA] = v[NC_ALA];
+    f[NF_ALD] = v[NC_ALD];
+    f[NF_BETAB] = v[NC_BETAB];
+    f[NF_D1SQ] = D1 * D1;
+    f[NF_D1SQFNS2] = D1 * D1 * v[NC_FN] * sq * sq;
+    f[NF_GNS] = v[NC_GN] * sq;
+    f[NF_HNS2] = v[NC_HN] * sq * sq;
+    f[NF_L2MN] = LOG2_10 * (-2.605 - 2.434 * ls + 5.71 * ls * ls);
+    f[NF_L2NN] = LOG2_10 * (-4.468 - 3.08 * ls + 1.035 * ls * ls);
+    f[NF_MUN] = v[NC_MUN];
+    f[NF_NUN] = v[NC_NUN];
+    f[NF_PNS] = v[NC_PN] * sq;
+    f[NF_ENS] = v[NC_EN] * sq;
+    f[NF_DNS] = v[NC_DN] * sq;
+    f[NF_TREE] = v[NC_TREE];
+    f[NF_D1P4] = v[NC_D1P4];
+    float* ff = fcoef_f + ((size_t)ci * NNODE + j) * NCP;
+    for (int q = 0; q < NCP; ++q) ff[q] = q < NF_COUNT ? (float)f[q] : 0.f;
   }
   // ---- P_kappa nodes: interpolation index z/zmax*255 (bispectrum.cu:535,956)
   {
@@ -425,7 +508,8 @@ __global__ void k_node_coefs(const CosmoDev* cos, const TablesDev* tab, double* 
 // wscale) so that FP32 products stay far from the float range limits, and
 // build the integrand constant blocks.
 __global__ void k_finish(const CosmoDev* cos, const EHConst* eh, const TablesDev* tab, double* ncoef, float* ncoef_f,
-                         double* wscale64, double* wscale32, CosmoK<double>* ck64, CosmoK<float>* ck32, int n) {
+                         float* fcoef_f, double* wscale64, double* wscale32, CosmoK<double>* ck64, CosmoK<float>* ck32,
+                         int n) {
   int ci = blockIdx.x;
   if (ci >= n) return;
   __shared__ double wmax;
@@ -443,6 +527,7 @@ __global__ void k_finish(const CosmoDev* cos, const EHConst* eh, const TablesDev
   for (int j = threadIdx.x; j < NNODE; j += blockDim.x) {
     size_t o = ((size_t)ci * NNODE + j) * NCP + NC_W;
     ncoef_f[o] = (float)(ncoef[o] / wmax);
+    fcoef_f[((size_t)ci * NNODE + j) * NCP + NF_W] = (float)(ncoef[o] / wmax);
   }
 }
 
@@ -480,7 +565,8 @@ void upload_gauss_nodes() {
 }
 
 cudaError_t build_tables(const CosmoDev* d_cos, EHConst* d_eh, const double* d_nz, int nz_stride, TablesDev* d_tab,
-                         double* d_ncoef, float* d_ncoef_f, double* d_hcoef, float* d_hcoef_f, double* d_wscale64,
+                         double* d_ncoef, float* d_ncoef_f, float* d_fcoef_f, double* d_hcoef, float* d_hcoef_f,
+                         double* d_wscale64,
                          double* d_wscale32, CosmoK<double>* d_ck64, CosmoK<float>* d_ck32, float4* d_plt, int n,
                          cudaStream_t s) {
   k_norm<<<n, 32, 0, s>>>(d_cos, d_eh, d_tab, n);
@@ -489,8 +575,9 @@ cudaError_t build_tables(const CosmoDev* d_cos, EHConst* d_eh, const double* d_n
   long warps = (long)n * NZ;
   int wpb = 4;
   k_rsigma<<<(unsigned)((warps + wpb - 1) / wpb), 32 * wpb, 0, s>>>(d_cos, d_eh, d_tab, n);
-  k_node_coefs<<<n, NNODE, 0, s>>>(d_cos, d_tab, d_ncoef, d_ncoef_f, d_hcoef, d_hcoef_f, n);
-  k_finish<<<n, NNODE, 0, s>>>(d_cos, d_eh, d_tab, d_ncoef, d_ncoef_f, d_wscale64, d_wscale32, d_ck64, d_ck32, n);
+  k_node_coefs<<<n, NNODE, 0, s>>>(d_cos, d_tab, d_ncoef, d_ncoef_f, d_fcoef_f, d_hcoef, d_hcoef_f, n);
+  k_finish<<<n, NNODE, 0, s>>>(d_cos, d_eh, d_tab, d_ncoef, d_ncoef_f, d_fcoef_f, d_wscale64, d_wscale32, d_ck64, d_ck32,
+                               n);
   k_plin_table<<<n, 256, 0, s>>>(d_cos, d_eh, d_plt, d_ck32, n);
   return cudaGetLastError();
 }
