@@ -36,7 +36,7 @@ METRIC = "Map3 triplets/s at <=1e-3 rel err vs FP64: surrogate+FP32 vs plain FP6
 ARCMIN = 2.9088820866e-4
 LHS_SEED = 20261203
 N_LHS = 4096
-SFU_PER_NODE = 28  # SFU ops (ex2/lg2/rcp.approx) per line-of-sight node of the FP32 BiHalofit evaluation
+SFU_PER_NODE = 27  # SFU ops (ex2/rcp.approx) per line-of-sight node of the FP32 BiHalofit evaluation (NF_* rows)
 NNODE = 96
 
 

@@ -300,62 +300,220 @@ __device__ __forceinline__ float plin_fast(const CosmoK<float>& K, const float* 
   return plin<float>(K, l * c[NF_HF], lg + c[NF_L2HF]);
 }
 
-// B at one node from its NF_* row (the bispec_eval formula, B4-B9 of
-// Takahashi et al. 2020, with the folded coefficients); W not applied.
-__device__ __forceinline__ float bispec_fast(const float* __restrict__ c, const TriF& T, const CosmoK<float>& K) {
-  typedef Mth<float> M;
-  float lq[3], P[3];
-#pragma unroll
-  for (int i = 0; i < 3; ++i) lq[i] = T.lg[i] + c[NF_L2S];
-  if (c[NF_TREE] != 0.f) {
-#pragma unroll
-    for (int i = 0; i < 3; ++i) P[i] = plin_fast(K, c, T.l[i], T.lg[i]);
-    return c[NF_D1P4] * 2.f * (T.f2t[0] * P[0] * P[1] + T.f2t[1] * P[1] * P[2] + T.f2t[2] * P[2] * P[0]);
-  }
-  // 1-halo term: 1 / ((a_n q^al + b_n q^be) (1 + 1/(c_n q))) per side
-  const float l2an = c[NF_ANA] - M::ex2(fmaf(c[NF_ANC], T.log2r1, c[NF_L2ANR]));
-  const float al = fminf(M::ex2(fmaf(c[NF_ALD], T.r2sq, c[NF_ALA])), K.alpha_max);
-  const float be = c[NF_BETAB] * T.pr2;
-  float bs1h = 1.f;
+// ---- packed FP32 pairs (fma/mul/add .f32x2: one issue slot for two lanes) --
+__device__ __forceinline__ float2 p2fma(float2 a, float2 b, float2 c) {
+  float2 d;
+  asm("{\n\t.reg .b64 ra, rb, rc, rd;\n\t"
+      "mov.b64 ra, {%2, %3};\n\tmov.b64 rb, {%4, %5};\n\tmov.b64 rc, {%6, %7};\n\t"
+      "fma.rn.f32x2 rd, ra, rb, rc;\n\tmov.b64 {%0, %1}, rd;\n\t}"
+      : "=f"(d.x), "=f"(d.y)
+      : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y), "f"(c.x), "f"(c.y));
+  return d;
+}
+__device__ __forceinline__ float2 p2mul(float2 a, float2 b) {
+  float2 d;
+  asm("{\n\t.reg .b64 ra, rb, rd;\n\t"
+      "mov.b64 ra, {%2, %3};\n\tmov.b64 rb, {%4, %5};\n\t"
+      "mul.rn.f32x2 rd, ra, rb;\n\tmov.b64 {%0, %1}, rd;\n\t}"
+      : "=f"(d.x), "=f"(d.y)
+      : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+  return d;
+}
+__device__ __forceinline__ float2 p2add(float2 a, float2 b) {
+  float2 d;
+  asm("{\n\t.reg .b64 ra, rb, rd;\n\t"
+      "mov.b64 ra, {%2, %3};\n\tmov.b64 rb, {%4, %5};\n\t"
+      "add.rn.f32x2 rd, ra, rb;\n\tmov.b64 {%0, %1}, rd;\n\t}"
+      : "=f"(d.x), "=f"(d.y)
+      : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+  return d;
+}
+__device__ __forceinline__ float2 p2sub(float2 a, float2 b) {
+  float2 d;
+  asm("{\n\t.reg .b64 ra, rb, rd;\n\t"
+      "mov.b64 ra, {%2, %3};\n\tmov.b64 rb, {%4, %5};\n\t"
+      "sub.rn.f32x2 rd, ra, rb;\n\tmov.b64 {%0, %1}, rd;\n\t}"
+      : "=f"(d.x), "=f"(d.y)
+      : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+  return d;
+}
+__device__ __forceinline__ float2 p2dup(float v) { return make_float2(v, v); }
+__device__ __forceinline__ float2 p2ex2(float2 a) { return make_float2(Mth<float>::ex2(a.x), Mth<float>::ex2(a.y)); }
+__device__ __forceinline__ float2 p2rcp(float2 a) { return make_float2(Mth<float>::rcp(a.x), Mth<float>::rcp(a.y)); }
+
+// The triangle of TriF with every field duplicated into both lanes of a pair.
+struct TriF2 {
+  float2 l[3], lg[3], l2[3];
+  float2 log2r1, r2sq, pr2;
+  float2 f2t[3];
+};
+__device__ __forceinline__ void trif2_from(const TriF& T, TriF2& D) {
 #pragma unroll
   for (int i = 0; i < 3; ++i) {
-    const float cq = c[NF_CNS] * T.l[i];
-    const float den = M::ex2(fmaf(al, lq[i], l2an)) + M::ex2(fmaf(be, lq[i], c[NF_L2BN]));
-    bs1h *= cq * M::rcp(den * (cq + 1.f));
+    D.l[i] = p2dup(T.l[i]);
+    D.lg[i] = p2dup(T.lg[i]);
+    D.l2[i] = p2dup(T.l2[i]);
+    D.f2t[i] = p2dup(T.f2t[i]);
+  }
+  D.log2r1 = p2dup(T.log2r1);
+  D.r2sq = p2dup(T.r2sq);
+  D.pr2 = p2dup(T.pr2);
+}
+
+// NF_* tables are stored as node pairs: coefficient k of node j at float
+// index ((j / 2) * NCP + k) * 2 + (j % 2), so that a pair's coefficient is
+// one float2 (the two lanes of the packed evaluation).
+__device__ __forceinline__ int nf_index(int j, int k) { return ((j >> 1) * NCP + k) * 2 + (j & 1); }
+
+// B at one node (the bispec_eval formula, B4-B9 of Takahashi et al. 2020,
+// with the folded NF_* coefficients) for the two nodes of pair c (c[k] =
+// coefficient k of both nodes), W not applied. Lanes are independent: the .x
+// lane is node 2p, the .y lane node 2p+1.
+// The triangle is a TriF2 (pairs held in registers) or a TriF (each value
+// duplicated where it is used): v2() gives the pair either way.
+__device__ __forceinline__ float2 v2(float x) { return p2dup(x); }
+__device__ __forceinline__ float2 v2(float2 x) { return x; }
+
+template <class TT>
+__device__ __forceinline__ float2 bispec_pair(const float2* __restrict__ c, const TT& T, const CosmoK<float>& K) {
+  typedef Mth<float> M;
+  const float2 one = p2dup(1.f);
+  float2 lq[3], P[3];
+  const float2 l2s = c[NF_L2S];
+#pragma unroll
+  for (int i = 0; i < 3; ++i) lq[i] = p2add(v2(T.lg[i]), l2s);
+  const float2 tree = c[NF_TREE];
+  if (tree.x != 0.f || tree.y != 0.f) {
+    // tree level beyond z = 10 (both lanes evaluated the same way)
+    const float2 d1p4 = c[NF_D1P4];
+    float2 r;
+    const float* cf = reinterpret_cast<const float*>(c);
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      float Ps[3];
+#pragma unroll
+      for (int i = 0; i < 3; ++i) {
+        const float li = h ? v2(T.l[i]).y : v2(T.l[i]).x, lgi = h ? v2(T.lg[i]).y : v2(T.lg[i]).x;
+        float cl[NCP];
+#pragma unroll
+        for (int k = 0; k < NCP; ++k) cl[k] = cf[2 * k + h];
+        Ps[i] = plin_fast(K, cl, li, lgi);
+      }
+      const float f0 = v2(T.f2t[0]).x, f1 = v2(T.f2t[1]).x, f2 = v2(T.f2t[2]).x;
+      const float v = (h ? d1p4.y : d1p4.x) * 2.f * (f0 * Ps[0] * Ps[1] + f1 * Ps[1] * Ps[2] + f2 * Ps[2] * Ps[0]);
+      if (h) r.y = v; else r.x = v;
+    }
+    return r;
+  }
+  // 1-halo term: 1 / ((a_n q^al + b_n q^be) (1 + 1/(c_n q))) per side
+  const float2 l2an = p2sub(c[NF_ANA], p2ex2(p2fma(c[NF_ANC], v2(T.log2r1), c[NF_L2ANR])));
+  float2 al = p2ex2(p2fma(c[NF_ALD], v2(T.r2sq), c[NF_ALA]));
+  al.x = fminf(al.x, K.alpha_max);
+  al.y = fminf(al.y, K.alpha_max);
+  const float2 be = p2mul(c[NF_BETAB], v2(T.pr2));
+  const float2 cns = c[NF_CNS], l2bn = c[NF_L2BN];
+  float2 bs1h = one;
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    const float2 cq = p2mul(cns, v2(T.l[i]));
+    const float2 den = p2add(p2ex2(p2fma(al, lq[i], l2an)), p2ex2(p2fma(be, lq[i], l2bn)));
+    bs1h = p2mul(bs1h, p2mul(cq, p2rcp(p2mul(den, p2add(cq, one)))));
   }
   // 3-halo term
 #pragma unroll
   for (int i = 0; i < 3; ++i) {
-    const float num = fmaf(c[NF_D1SQFNS2], T.l2[i], c[NF_D1SQ]);
-    const float den = fmaf(c[NF_HNS2], T.l2[i], fmaf(c[NF_GNS], T.l[i], 1.f));
-    const float a = num * M::rcp(den) * plin_fast(K, c, T.l[i], T.lg[i]);
-    const float x = c[NF_PNS] * T.l[i];
-    const float x3 = x * x * x;
-    const float mq = M::ex2(fmaf(c[NF_MUN], lq[i], c[NF_L2MN])) + M::ex2(fmaf(c[NF_NUN], lq[i], c[NF_L2NN]));
-    P[i] = fmaf(x3, M::rcp(mq * (x3 + 1.f)), a);
+    const float2 num = p2fma(c[NF_D1SQFNS2], v2(T.l2[i]), c[NF_D1SQ]);
+    const float2 den = p2fma(c[NF_HNS2], v2(T.l2[i]), p2fma(c[NF_GNS], v2(T.l[i]), one));
+    // linear P(k) of the two nodes (table lookups per lane)
+    float2 pl;
+    {
+      constexpr float INV = (float)((PLT_N - 1) / (PLT_HI - PLT_LO));
+      const float2 t2 = p2fma(v2(T.lg[i]), p2dup(INV), c[NF_TOFF]);
+      if (K.plt) {
+        float tt[2] = {t2.x, t2.y}, r[2];
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+          const float t = fminf(fmaxf(tt[h], 0.f), (float)(PLT_N - 1) - 1e-3f);
+          const float tm = __fadd_rd(t, 12582912.f);  // 1.5 * 2^23 + floor(t)
+          const int ix = __float_as_int(tm) - 0x4B400000;
+          const float f = t - (tm - 12582912.f);
+          const float4 q = reinterpret_cast<const float4*>(K.plt)[ix];
+          r[h] = M::ex2(fmaf(f, fmaf(f, fmaf(f, q.w, q.z), q.y), q.x));
+        }
+        pl = make_float2(r[0], r[1]);
+      } else {
+        const float2 hf = c[NF_HF], l2hf = c[NF_L2HF];
+        pl.x = plin<float>(K, v2(T.l[i]).x * hf.x, v2(T.lg[i]).x + l2hf.x);
+        pl.y = plin<float>(K, v2(T.l[i]).y * hf.y, v2(T.lg[i]).y + l2hf.y);
+      }
+    }
+    const float2 a = p2mul(p2mul(num, p2rcp(den)), pl);
+    const float2 x = p2mul(c[NF_PNS], v2(T.l[i]));
+    const float2 x3 = p2mul(p2mul(x, x), x);
+    const float2 mq = p2add(p2ex2(p2fma(c[NF_MUN], lq[i], c[NF_L2MN])), p2ex2(p2fma(c[NF_NUN], lq[i], c[NF_L2NN])));
+    P[i] = p2fma(x3, p2rcp(p2mul(mq, p2add(x3, one))), a);
   }
-  const float dn = c[NF_DNS], en = c[NF_ENS];
-  float bs3h = fmaf(dn, T.l[2], T.f2t[0]) * P[0] * P[1];
-  bs3h = fmaf(fmaf(dn, T.l[0], T.f2t[1]) * P[1], P[2], bs3h);
-  bs3h = fmaf(fmaf(dn, T.l[1], T.f2t[2]) * P[2], P[0], bs3h);
-  const float e3 = fmaf(en, T.l[0], 1.f) * fmaf(en, T.l[1], 1.f) * fmaf(en, T.l[2], 1.f);
-  return fmaf(2.f * bs3h, M::rcp(e3), bs1h);
+  const float2 dn = c[NF_DNS], en = c[NF_ENS];
+  float2 bs3h = p2mul(p2mul(p2fma(dn, v2(T.l[2]), v2(T.f2t[0])), P[0]), P[1]);
+  bs3h = p2fma(p2mul(p2fma(dn, v2(T.l[0]), v2(T.f2t[1])), P[1]), P[2], bs3h);
+  bs3h = p2fma(p2mul(p2fma(dn, v2(T.l[1]), v2(T.f2t[2])), P[2]), P[0], bs3h);
+  const float2 e3 = p2mul(p2mul(p2fma(en, v2(T.l[0]), one), p2fma(en, v2(T.l[1]), one)), p2fma(en, v2(T.l[2]), one));
+  return p2fma(p2mul(p2dup(2.f), bs3h), p2rcp(e3), bs1h);
 }
 
-// W B at node j of an NF_* table (node-major, 16-byte rows)
+// W B at the two nodes of pair p of a pair-interleaved NF_* table
+template <class TT>
+__device__ __forceinline__ float2 bispec_pair_node(const float* __restrict__ nf, int p, const TT& T,
+                                                   const CosmoK<float>& K) {
+  const float2* c = reinterpret_cast<const float2*>(nf) + (size_t)p * NCP;
+  return p2mul(c[NF_W], bispec_pair(c, T, K));
+}
+
+// W B at node j of a pair-interleaved NF_* table, one lane per node
+// (the scalar form of bispec_pair, for callers with one point per lane)
 __device__ __forceinline__ float bispec_node_fast(const float* __restrict__ nf, int j, const TriF& T,
                                                   const CosmoK<float>& K) {
+  typedef Mth<float> M;
   float c[NCP];
-  const float4* v = reinterpret_cast<const float4*>(nf + j * NCP);
 #pragma unroll
-  for (int q = 0; q < NCP / 4; ++q) {
-    float4 t = v[q];
-    c[4 * q] = t.x;
-    c[4 * q + 1] = t.y;
-    c[4 * q + 2] = t.z;
-    c[4 * q + 3] = t.w;
+  for (int k = 0; k < NCP; ++k) c[k] = nf[nf_index(j, k)];
+  float lq[3], P[3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i) lq[i] = T.lg[i] + c[NF_L2S];
+  float B;
+  if (c[NF_TREE] != 0.f) {
+#pragma unroll
+    for (int i = 0; i < 3; ++i) P[i] = plin_fast(K, c, T.l[i], T.lg[i]);
+    B = c[NF_D1P4] * 2.f * (T.f2t[0] * P[0] * P[1] + T.f2t[1] * P[1] * P[2] + T.f2t[2] * P[2] * P[0]);
+  } else {
+    const float l2an = c[NF_ANA] - M::ex2(fmaf(c[NF_ANC], T.log2r1, c[NF_L2ANR]));
+    const float al = fminf(M::ex2(fmaf(c[NF_ALD], T.r2sq, c[NF_ALA])), K.alpha_max);
+    const float be = c[NF_BETAB] * T.pr2;
+    float bs1h = 1.f;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      const float cq = c[NF_CNS] * T.l[i];
+      const float den = M::ex2(fmaf(al, lq[i], l2an)) + M::ex2(fmaf(be, lq[i], c[NF_L2BN]));
+      bs1h *= cq * M::rcp(den * (cq + 1.f));
+    }
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      const float num = fmaf(c[NF_D1SQFNS2], T.l2[i], c[NF_D1SQ]);
+      const float den = fmaf(c[NF_HNS2], T.l2[i], fmaf(c[NF_GNS], T.l[i], 1.f));
+      const float a = num * M::rcp(den) * plin_fast(K, c, T.l[i], T.lg[i]);
+      const float x = c[NF_PNS] * T.l[i];
+      const float x3 = x * x * x;
+      const float mq = M::ex2(fmaf(c[NF_MUN], lq[i], c[NF_L2MN])) + M::ex2(fmaf(c[NF_NUN], lq[i], c[NF_L2NN]));
+      P[i] = fmaf(x3, M::rcp(mq * (x3 + 1.f)), a);
+    }
+    const float dn = c[NF_DNS], en = c[NF_ENS];
+    float bs3h = fmaf(dn, T.l[2], T.f2t[0]) * P[0] * P[1];
+    bs3h = fmaf(fmaf(dn, T.l[0], T.f2t[1]) * P[1], P[2], bs3h);
+    bs3h = fmaf(fmaf(dn, T.l[1], T.f2t[2]) * P[2], P[0], bs3h);
+    const float e3 = fmaf(en, T.l[0], 1.f) * fmaf(en, T.l[1], 1.f) * fmaf(en, T.l[2], 1.f);
+    B = fmaf(2.f * bs3h, M::rcp(e3), bs1h);
   }
-  return c[NF_W] * bispec_fast(c, T, K);
+  return c[NF_W] * B;
 }
 
 // Mid-bin two-point interpolation of a z table at fractional bin position fb

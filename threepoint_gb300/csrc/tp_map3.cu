@@ -26,7 +26,10 @@
 #define TP_MAP3_MINB 3
 #endif
 #ifndef TP_MAP3_UNROLL
-#define TP_MAP3_UNROLL 4
+#define TP_MAP3_UNROLL 2
+#endif
+#ifndef TP_MAP3_DUP_IN_LOOP
+#define TP_MAP3_DUP_IN_LOOP 0
 #endif
 #define TP_PRAGMA(x) _Pragma(#x)
 #define TP_UNROLL(n) TP_PRAGMA(unroll n)
@@ -189,19 +192,37 @@ struct Map3Policy {
   __device__ void group(const char* recp, int g, double* pv) {
     const Rec& r = *(const Rec*)recp;
     const CosmoK<R> K = *s_ck;
-    KSum<R> acc;
     const int j0 = g * NPG;
-    TP_UNROLL(TP_MAP3_UNROLL)
-    for (int j = j0; j < j0 + NPG; ++j) {
-      R v;
-      if constexpr (sizeof(R) == 4)
-        v = bispec_node_fast(s_nc, j, r.tri, K);
-      else
-        v = bispec_node<R>(s_nc, j, r.tri, K);
-      if (v != v) v = (R)0;  // NaN in bispec -> 0 (bispectrum.cu:327-331)
-      acc.add(v);
+    if constexpr (sizeof(R) == 4) {
+      // two nodes per step in packed FP32 pairs; Kahan sum per lane
+#if TP_MAP3_DUP_IN_LOOP
+      const TriF& T2 = r.tri;  // pairs formed where used
+#else
+      TriF2 T2;  // pairs held in registers across the node loop
+      trif2_from(r.tri, T2);
+#endif
+      float2 s = make_float2(0.f, 0.f), cmp = make_float2(0.f, 0.f);
+      TP_UNROLL(TP_MAP3_UNROLL)
+      for (int p = j0 / 2; p < (j0 + NPG) / 2; ++p) {
+        float2 v = bispec_pair_node(s_nc, p, T2, K);
+        if (v.x != v.x) v.x = 0.f;  // NaN in bispec -> 0 (bispectrum.cu:327-331)
+        if (v.y != v.y) v.y = 0.f;
+        const float2 y = p2sub(v, cmp);
+        const float2 t = p2add(s, y);
+        cmp = p2sub(p2sub(t, s), y);
+        s = t;
+      }
+      pv[0] = (double)s.x + (double)s.y;
+    } else {
+      KSum<R> acc;
+      TP_UNROLL(TP_MAP3_UNROLL)
+      for (int j = j0; j < j0 + NPG; ++j) {
+        R v = bispec_node<R>(s_nc, j, r.tri, K);
+        if (v != v) v = (R)0;  // NaN in bispec -> 0 (bispectrum.cu:327-331)
+        acc.add(v);
+      }
+      pv[0] = (double)acc.s;
     }
-    pv[0] = (double)acc.s;
   }
 
   __device__ bool is_live(const char* recp) const { return ((const Rec*)recp)->live != 0; }

@@ -456,8 +456,9 @@ __global__ void k_node_coefs(const CosmoDev* cos, const TablesDev* tab, double* 
     f[NF_DNS] = v[NC_DN] * sq;
     f[NF_TREE] = v[NC_TREE];
     f[NF_D1P4] = v[NC_D1P4];
-    float* ff = fcoef_f + ((size_t)ci * NNODE + j) * NCP;
-    for (int q = 0; q < NCP; ++q) ff[q] = q < NF_COUNT ? (float)f[q] : 0.f;
+    // pair-interleaved layout (nf_index): nodes 2p and 2p+1 side by side
+    float* ff = fcoef_f + (size_t)ci * NNODE * NCP;
+    for (int q = 0; q < NCP; ++q) ff[nf_index(j, q)] = q < NF_COUNT ? (float)f[q] : 0.f;
   }
   // ---- P_kappa nodes: interpolation index z/zmax*255 (bispectrum.cu:535,956)
   {
@@ -527,7 +528,7 @@ __global__ void k_finish(const CosmoDev* cos, const EHConst* eh, const TablesDev
   for (int j = threadIdx.x; j < NNODE; j += blockDim.x) {
     size_t o = ((size_t)ci * NNODE + j) * NCP + NC_W;
     ncoef_f[o] = (float)(ncoef[o] / wmax);
-    fcoef_f[((size_t)ci * NNODE + j) * NCP + NF_W] = (float)(ncoef[o] / wmax);
+    fcoef_f[(size_t)ci * NNODE * NCP + nf_index(j, NF_W)] = (float)(ncoef[o] / wmax);
   }
 }
 
