@@ -146,9 +146,16 @@ def run_ours(args):
         import torch.distributed as dist
 
         dist.init_process_group("nccl")
-    ctx = tp.Context(local)
-    ctx.set_limits(args.region_cap)
-    stream = torch.cuda.ExternalStream(ctx.stream_handle, device=local)
+    # two contexts (own stream, tables and region stores) take alternate
+    # batches: one batch's table build and launch tail overlap the other's
+    # integrals. --no-pipeline runs every step alone on one context.
+    nctx = 1 if args.no_pipeline else 2
+    ctxs = [tp.Context(local) for _ in range(nctx)]
+    for c in ctxs:
+        c.set_limits(args.region_cap)
+    ctx = ctxs[0]
+    streams = [torch.cuda.ExternalStream(c.stream_handle, device=local) for c in ctxs]
+    stream = streams[0]
     cosmos_all = lhs_cosmologies()
     zs, ns = nz_config()
     nz = tp.rebin_n_of_z(zs, ns, 256, 3.0)
@@ -159,11 +166,15 @@ def run_ours(args):
     dev = torch.device("cuda", local)
     job_cosmo = torch.arange(C, dtype=torch.int32, device=dev).repeat_interleave(nt)
     job_theta = torch.tensor(np.tile(th, (C, 1)), dtype=torch.float64, device=dev)
-    out = torch.zeros(nj, dtype=torch.float64, device=dev)
-    err = torch.zeros_like(out)
-    nev = torch.zeros(nj, dtype=torch.int64, device=dev)
-    nlive = torch.zeros(nj, dtype=torch.int64, device=dev)
-    status = torch.zeros(nj, dtype=torch.int32, device=dev)
+
+    def buffers():
+        o = torch.zeros(nj, dtype=torch.float64, device=dev)
+        return dict(out=o, err=torch.zeros_like(o), nev=torch.zeros(nj, dtype=torch.int64, device=dev),
+                    nlive=torch.zeros(nj, dtype=torch.int64, device=dev),
+                    status=torch.zeros(nj, dtype=torch.int32, device=dev))
+
+    bufs = [buffers() for _ in ctxs]
+    out, err, nev, nlive, status = (bufs[0][k] for k in ("out", "err", "nev", "nlive", "status"))
     lmax = 0.0 if args.lmax == "ref" else float(args.lmax)
     flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=dev)  # > 129 MB L2
 
@@ -177,23 +188,28 @@ def run_ours(args):
 
     order = [None]
 
-    def one_step(step, timing):
+    def one_step(step, k, timing=None, flush_first=False):
+        """Batch `step` on context k: L2 flush (optional), table build, all
+        C x 220 integrals; all on context k's stream."""
+        c, st, b = ctxs[k], streams[k], bufs[k]
         batch = cosmo_batch(step)
         ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
-        with torch.cuda.stream(stream):
-            ev[0].record(stream)
-            ctx.set_cosmologies(batch, nz)
-            ev[1].record(stream)
-            ctx.map3_jobs_device(job_cosmo, job_theta, out, err, nev, status, lMax=lmax, rel_tol=1e-4,
-                                 precision=tp.FP32, nlive=nlive, job_order=order[0])
-            ev[2].record(stream)
+        with torch.cuda.stream(st):
+            if flush_first:
+                flush.zero_()  # L2 flush between steps (on this step's stream)
+            ev[0].record(st)
+            c.set_cosmologies(batch, nz)
+            ev[1].record(st)
+            c.map3_jobs_device(job_cosmo, job_theta, b["out"], b["err"], b["nev"], b["status"], lMax=lmax,
+                               rel_tol=1e-4, precision=tp.FP32, nlive=b["nlive"], job_order=order[0])
+            ev[2].record(st)
         if timing is not None:
             timing.append(ev)
 
     # warm-up; after the first warm-up step the jobs are ordered longest-first
     # by the per-triplet cost seen there (what tp_map3_batch does internally)
     for s in range(args.warmup):
-        one_step(s, None)
+        one_step(s, s % nctx)
         if s == 0 and not args.no_order:
             torch.cuda.synchronize()
             cost = nev.view(C, nt).double().mean(0)
@@ -205,32 +221,51 @@ def run_ours(args):
         dist.barrier()
     sampler = ClockSampler(local)
     sampler.start()
-    timings = []
-    live_total = 0
     torch.cuda.synchronize()
     t0 = time.perf_counter()
+    start = torch.cuda.Event(enable_timing=True)
+    start.record(streams[0])
+    for st in streams[1:]:
+        st.wait_event(start)
+    bad = 0
     for s in range(args.steps):
-        flush.zero_()  # L2 flush between steps (outside the per-step events)
+        one_step(args.warmup + s, s % nctx, flush_first=True)
+        if nctx == 1:
+            torch.cuda.synchronize()
+    ends = []
+    for st in streams:
+        e = torch.cuda.Event(enable_timing=True)
+        e.record(st)
+        ends.append(e)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    clocks = sampler.stop()
+    tot_ms = max(start.elapsed_time(e) for e in ends)
+    for b in bufs:
+        bad += int((b["status"] != 0).sum().item())
+    if bad:
+        print(f"warning: {bad} integrals hit a cap in the last steps", file=sys.stderr)
+    if dist:
+        tt = torch.tensor([tot_ms], device=dev)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        tot_ms = float(tt.item())
+
+    # kernel time for the roofline: k_map3 launches timed alone (no overlap),
+    # outside the timed region
+    timings = []
+    live_total = 0
+    n_roof = min(args.steps, 3)
+    for s in range(n_roof):
+        flush.zero_()
         torch.cuda.synchronize()
-        one_step(args.warmup + s, timings)
+        one_step(args.warmup + s, 0, timings)
         torch.cuda.synchronize()
         live_total += int(nlive.sum().item())
         if args.dump_costs and s == 0:
             np.savez(args.dump_costs, theta=np.tile(th, (C, 1)), neval=nev.cpu().numpy(), nlive=nlive.cpu().numpy(),
                      value=out.cpu().numpy())
-        bad = int((status != 0).sum().item())
-        if bad:
-            print(f"warning: {bad} integrals hit a cap in step {s}", file=sys.stderr)
-    torch.cuda.synchronize()
-    wall = time.perf_counter() - t0
-    clocks = sampler.stop()
-    step_ms = [t[0].elapsed_time(t[2]) for t in timings]
     map3_ms = [t[1].elapsed_time(t[2]) for t in timings]
-    tot_ms = sum(step_ms)
-    if dist:
-        tt = torch.tensor([tot_ms], device=dev)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        tot_ms = float(tt.item())
+    build_ms = [t[0].elapsed_time(t[1]) for t in timings]
     integrals = nj * args.steps * world
     value = integrals / (tot_ms * 1e-3)
 
@@ -275,7 +310,7 @@ def run_ours(args):
 
     # roofline of the dominant kernel (k_map3<float>): SFU ops of the live points
     sfu_peak, f32_peak, f64_peak = tp.pipe_peaks(local)
-    live_per_launch = live_total / args.steps
+    live_per_launch = live_total / n_roof
     map3_avg_s = statistics.mean(map3_ms) * 1e-3
     achieved = live_per_launch * NNODE * SFU_PER_NODE / map3_avg_s
 
@@ -300,6 +335,9 @@ def run_ours(args):
                    "cosmologies_per_step": C, "triplets": nt, "rel_tol": 1e-4,
                    "l_range": "[1, 10/theta_min]" if lmax == 0 else f"[1, {lmax:g}]",
                    "l2": "flushed between steps (256 MB write)", "parallelism": f"replicas x{world}",
+                   "pipeline": "1 context" if nctx == 1 else
+                   "2 contexts on 2 streams, alternate batches (table build and launch tail overlap)",
+                   "table_build_ms_alone": statistics.mean(build_ms), "map3_ms_alone": statistics.mean(map3_ms),
                    "job_order": "none" if args.no_order else "longest-first by warm-up cost per triplet",
                    "max_rel_err_fp32_vs_fp64": max_rel, "fp64_check_integrals": int(v64.size),
                    "zero_valued_agree": zeros_agree},
@@ -384,7 +422,7 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--cosmo-per-step", type=int, default=16)
+    ap.add_argument("--cosmo-per-step", type=int, default=64)
     ap.add_argument("--lmax", default="ref")
     ap.add_argument("--cpu-sample", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -392,6 +430,7 @@ def main():
     ap.add_argument("--dump-costs", default="")
     ap.add_argument("--no-order", action="store_true")
     ap.add_argument("--no-fp64-plain", action="store_true", help="skip the plain FP64 comparison run")
+    ap.add_argument("--no-pipeline", action="store_true", help="one context, steps run one after another")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
     res = run_reference(args) if args.impl == "reference" else run_ours(args)

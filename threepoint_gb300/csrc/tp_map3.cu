@@ -26,10 +26,10 @@
 #define TP_MAP3_MINB 3
 #endif
 #ifndef TP_MAP3_UNROLL
-#define TP_MAP3_UNROLL 2
+#define TP_MAP3_UNROLL 1
 #endif
 #ifndef TP_MAP3_DUP_IN_LOOP
-#define TP_MAP3_DUP_IN_LOOP 0
+#define TP_MAP3_DUP_IN_LOOP 1
 #endif
 #define TP_PRAGMA(x) _Pragma(#x)
 #define TP_UNROLL(n) TP_PRAGMA(unroll n)
