@@ -36,6 +36,11 @@ METRIC = "Map3 triplets/s at <=1e-3 rel err vs FP64: surrogate+FP32 vs plain FP6
 ARCMIN = 2.9088820866e-4
 LHS_SEED = 20261203
 N_LHS = 4096
+# DRAM bytes (read + write) of one k_map3<float> launch per integral, from
+# ncu dram__bytes_read.sum + dram__bytes_write.sum of a 880-integral launch
+# (4 LHS cosmologies x 220 triplets: 71.2 + 228.3 MB); the region-store
+# traffic grows with the number of integrals
+TRAFFIC_PER_INTEGRAL = (71.241984e6 + 228.270848e6) / 880
 SFU_PER_NODE = 27  # SFU ops (ex2/rcp.approx) per line-of-sight node of the FP32 BiHalofit evaluation (NF_* rows)
 NNODE = 96
 
@@ -344,7 +349,8 @@ def run_ours(args):
         "e2e": {"value": e2e_val, "unit": "triplets/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": 8 * args.steps,  # 7 table-build kernels + k_map3 per step
         "roofline": {"bound": "sfu", "achieved": achieved / 1e9, "peak": sfu_peak / 1e9, "unit": "Gop/s",
-                     "frac": achieved / sfu_peak, "traffic": None,
+                     "frac": achieved / sfu_peak, "traffic": TRAFFIC_PER_INTEGRAL * nj,
+                     "traffic_unit": "bytes per launch (ncu, 880-integral capture scaled by integrals)",
                      "peak_source": "measured now by tp_pipe_peaks (ex2.approx.f32 loop, whole device)",
                      "kernel": "k_map3<float>", "kernel_ms_per_launch": map3_avg_s * 1e3,
                      "fp32_fma_peak_tflops": f32_peak / 1e12, "fp64_fma_peak_tflops": f64_peak / 1e12},

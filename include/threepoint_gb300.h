@@ -243,6 +243,26 @@ int tp_cov_total_batch(tp_ctx* ctx, int cosmo_index, int term, int geometry, dou
 int tp_cov_term_batch(tp_ctx* ctx, int cosmo_index, int term, int geometry, double theta_max, double area,
                       const double* th6, int n, int precision, double* out, int* n_capped);
 
+/* ---- likelihood of <Map^3> model vectors -------------------------------- */
+
+/* Gaussian likelihood of the reference's cosmosis likelihood module
+ * (cosmosis/threepoint_likelihood.py:8-58): chi2 = (m - d)^T C^-1 (m - d),
+ * log L = -chi2 / 2. tp_likelihood_create factors the n x n covariance (FP64
+ * Cholesky on the GPU) once; TP_ERR_ARG if it is not positive definite (the
+ * reference inverts any invertible matrix with numpy). */
+typedef struct tp_likelihood tp_likelihood;
+int tp_likelihood_create(int device, const double* data, const double* cov, int n, tp_likelihood** out);
+void tp_likelihood_destroy(tp_likelihood* lk);
+const char* tp_likelihood_last_error(const tp_likelihood* lk);
+/* C^-1 (n x n, row-major), the file the reference writes as cov_inv */
+int tp_likelihood_cov_inv(tp_likelihood* lk, double* out);
+/* chi2 of n_models model vectors models[n_models][n] (host buffers) */
+int tp_likelihood_chi2(tp_likelihood* lk, const double* models, int n_models, double* chi2_out);
+/* Device-resident form, asynchronous on `stream` (a cudaStream_t; NULL = the
+ * likelihood's own stream): model b at models_device + b * ld, ld >= n. */
+int tp_likelihood_chi2_device(tp_likelihood* lk, const double* models_device, int n_models, long ld,
+                              double* chi2_device, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -170,6 +170,14 @@ def lib():
         L.tp_cov_params_from_file.argtypes = [C.c_char_p, C.POINTER(_CovParams)]
         L.tp_gamma_config_from_file.argtypes = [C.c_char_p, C.POINTER(_GammaConfig)]
         L.tp_gamma_triangles.argtypes = [C.POINTER(_GammaConfig), dp, dp]
+        L.tp_likelihood_create.argtypes = [i, dp, dp, i, C.POINTER(p)]
+        L.tp_likelihood_destroy.argtypes = [p]
+        L.tp_likelihood_destroy.restype = None
+        L.tp_likelihood_last_error.argtypes = [p]
+        L.tp_likelihood_last_error.restype = C.c_char_p
+        L.tp_likelihood_cov_inv.argtypes = [p, dp]
+        L.tp_likelihood_chi2.argtypes = [p, dp, i, dp]
+        L.tp_likelihood_chi2_device.argtypes = [p, p, i, l, p, p]
         _lib = L
     return _lib
 
@@ -412,6 +420,57 @@ class Context:
 
     def T4_total(self, th123, th456, **kw):
         return float(self.cov_total(4, [th123], [th456], **kw)[0])
+
+
+class Likelihood:
+    """Gaussian likelihood of <Map^3> model vectors against a measurement
+    (cosmosis/threepoint_likelihood.py:8-58): chi2 = (m-d)^T C^-1 (m-d),
+    log L = -chi2/2. The covariance is factored once on the GPU."""
+
+    def __init__(self, data, cov, device=0):
+        d = _arr(data).reshape(-1)
+        c = _arr(cov).reshape(len(d), len(d))
+        self.n = len(d)
+        self._h = C.c_void_p(0)
+        st = lib().tp_likelihood_create(device, _dp(d), _dp(c), self.n, C.byref(self._h))
+        if st == TP_ERR_ARG:
+            raise ThreepointError(st, "covariance is not positive definite (or has non-finite entries)")
+        _check(None, st)
+
+    def cov_inv(self):
+        out = np.zeros((self.n, self.n))
+        self._chk(lib().tp_likelihood_cov_inv(self._h, _dp(out)))
+        return out
+
+    def chi2(self, models):
+        m = _arr(models).reshape(-1, self.n)
+        out = np.zeros(len(m))
+        self._chk(lib().tp_likelihood_chi2(self._h, _dp(m), len(m), _dp(out)))
+        return out
+
+    def loglike(self, models):
+        return -0.5 * self.chi2(models)
+
+    def chi2_device(self, models, out, stream=None):
+        """models: CUDA float64 tensor [B, >=n] (row stride >= n); out: [B]."""
+        self._chk(lib().tp_likelihood_chi2_device(self._h, C.c_void_p(models.data_ptr()), int(models.shape[0]),
+                                                  int(models.stride(0)), C.c_void_p(out.data_ptr()),
+                                                  C.c_void_p(stream) if stream else None))
+
+    def _chk(self, st):
+        if st != TP_OK:
+            raise ThreepointError(st, lib().tp_likelihood_last_error(self._h).decode())
+
+    def close(self):
+        if self._h:
+            lib().tp_likelihood_destroy(self._h)
+            self._h = C.c_void_p(0)
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def ogata_weights():
