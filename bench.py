@@ -422,6 +422,111 @@ def run_reference(args):
     }
 
 
+COSMO_FID = dict(h=0.7, sigma8=0.8, omb=0.048, omc=0.3 - 0.048, ns=0.96, w=-1.0, om=0.3, ow=0.7, zmax=3.0)
+
+
+def _rel_stats(a, b):
+    """per-output relative differences |a-b|/|b| over outputs with |b| > 0"""
+    a, b = np.asarray(a).reshape(-1), np.asarray(b).reshape(-1)
+    m = np.abs(b) > 0
+    r = np.abs(a[m] - b[m]) / np.abs(b[m])
+    return {"max": float(r.max()) if r.size else None, "median": float(np.median(r)) if r.size else None,
+            "outputs": int(m.sum())}
+
+
+def run_gamma(args):
+    """Shear 3PCF on the (r, u, v) grid of calculateGamma: 10 log r bins on
+    0.1-100', 10 u bins on [0, 1], 10 v bins on [-1, 1] (bin centres), all four
+    natural components, centroid convention; FP32 integrand timed, FP64 on a
+    subset for the per-output error."""
+    import torch
+
+    import threepoint_gb300 as tp
+
+    rank, world, local = dist_env()
+    if rank != 0:
+        return None
+    torch.cuda.set_device(local)
+    ctx = tp.Context(local)
+    zs, ns = nz_config()
+    ctx.set_cosmology(tp.cosmology(**COSMO_FID), tp.rebin_n_of_z(zs, ns, 256, 3.0))
+    cfg = tp.configGamma(10, 10, 10, 0.0, 1.0, -1.0, 1.0, 0.1, 100.0)
+    x, _ = cfg.triangles()
+    n = len(x) if args.gamma_triangles <= 0 else min(len(x), args.gamma_triangles)
+    x = x[:n]
+    ctx.gamma_batch(x[: min(n, 8)], precision=tp.FP32)  # warm-up
+    times = []
+    for _ in range(args.steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        g32 = ctx.gamma_batch(x, precision=tp.FP32)
+        times.append(time.perf_counter() - t0)
+    sub = np.arange(0, n, max(1, n // args.gamma_fp64_sample))
+    t0 = time.perf_counter()
+    g64 = ctx.gamma_batch(x[sub], precision=tp.FP64)
+    t64 = time.perf_counter() - t0
+    err = _rel_stats(np.stack([g32[sub].real, g32[sub].imag]), np.stack([g64.real, g64.imag]))
+    tot = sum(times)
+    return {"metric": "Gamma_0..3 triangles/s (4 natural components, rel. tol 1e-3)", "value": n * args.steps / tot,
+            "unit": "triangles/s", "n_gpus": 1, "steps": args.steps, "warmup": 1, "ms_per_step": tot / args.steps * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": f"calculateGamma grid: {n} (r,u,v) bin centres x 4 components, fiducial cosmology",
+                       "timing": "host API tp_gamma_batch per step (host inputs and outputs)"},
+            "fp64": {"triangles": int(len(sub)), "triangles_per_s": len(sub) / t64,
+                     "rel_err_fp32_vs_fp64": err}}
+
+
+def run_cov(args):
+    """<Map^3> covariance T1 + T2 (square 10x10 deg^2 window) and T4 (infinite
+    geometry with the survey area) for a seeded sample of the 24310 (triplet,
+    triplet) pairs of the 220 triplets; sigma_eps 0.3, n_gal 10 arcmin^-2.
+    Integrals that reach the region cap are counted, not fatal."""
+    import torch
+
+    import threepoint_gb300 as tp
+
+    rank, world, local = dist_env()
+    if rank != 0:
+        return None
+    torch.cuda.set_device(local)
+    ctx = tp.Context(local)
+    zs, ns = nz_config()
+    ctx.set_shape_noise(0.3, 10 / ARCMIN ** 2, False)
+    ctx.set_cosmology(tp.cosmology(**COSMO_FID), tp.rebin_n_of_z(zs, ns, 256, 3.0))
+    th = thetas_220()
+    pairs = [(i, j) for i in range(len(th)) for j in range(i, len(th))]
+    rng = np.random.default_rng(LHS_SEED)
+    pick = rng.choice(len(pairs), size=min(args.cov_pairs, len(pairs)), replace=False)
+    A = np.array([th[pairs[k][0]] for k in pick])
+    B = np.array([th[pairs[k][1]] for k in pick])
+    deg = 0.017453
+    kw = dict(thetaMax=10 * deg, area=100 * deg * deg)
+    terms = (("T1", 1, tp.GEOM_SQUARE), ("T2", 2, tp.GEOM_SQUARE), ("T4", 4, tp.GEOM_INFINITE))
+    res, t, capped = {}, {}, {}
+    for name, term, geom in terms:
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        res[name] = ctx.cov_total(term, A, B, geometry=geom, precision=tp.FP32, check=False, **kw)
+        t[name] = time.perf_counter() - t0
+        capped[name] = ctx.last_capped
+    n64 = min(len(pick), args.cov_fp64_pairs)
+    err, t64 = {}, {}
+    for name, term, geom in terms:
+        t0 = time.perf_counter()
+        r64 = ctx.cov_total(term, A[:n64], B[:n64], geometry=geom, precision=tp.FP64, check=False, **kw)
+        t64[name] = time.perf_counter() - t0
+        err[name] = _rel_stats(res[name][:n64], r64)
+    tot = sum(t.values())
+    return {"metric": "<Map^3> covariance entries/s (T1+T2 square 10x10 deg^2, T4 infinite with area)",
+            "value": len(pick) / tot, "unit": "entries/s", "n_gpus": 1, "steps": 1, "warmup": 0,
+            "ms_per_step": tot * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic",
+            "config": {"workload": f"{len(pick)} of the 24310 triplet pairs of 220 triplets (seeded sample)",
+                       "seconds_per_term": t, "timing": "host API tp_cov_total_batch",
+                       "integrals_at_region_cap": capped},
+            "fp64": {"pairs": n64, "seconds_per_term": t64, "rel_err_fp32_vs_fp64": err}}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -437,9 +542,22 @@ def main():
     ap.add_argument("--no-order", action="store_true")
     ap.add_argument("--no-fp64-plain", action="store_true", help="skip the plain FP64 comparison run")
     ap.add_argument("--no-pipeline", action="store_true", help="one context, steps run one after another")
+    ap.add_argument("--workload", default="map3", choices=["map3", "gamma", "cov"],
+                    help="map3: the headline metric; gamma / cov: the shear-3PCF grid and covariance configurations")
+    ap.add_argument("--gamma-triangles", type=int, default=0, help="first N triangles of the grid (0 = all 1000)")
+    ap.add_argument("--gamma-fp64-sample", type=int, default=20)
+    ap.add_argument("--cov-pairs", type=int, default=24)
+    ap.add_argument("--cov-fp64-pairs", type=int, default=4)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
-    res = run_reference(args) if args.impl == "reference" else run_ours(args)
+    if args.impl == "reference":
+        res = run_reference(args)
+    elif args.workload == "gamma":
+        res = run_gamma(args)
+    elif args.workload == "cov":
+        res = run_cov(args)
+    else:
+        res = run_ours(args)
     if res is not None:
         print(json.dumps(res))
 

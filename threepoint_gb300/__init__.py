@@ -392,15 +392,20 @@ class Context:
 
     # -- covariance (cuda_version/apertureStatisticsCovariance.cu:272-683) --
     def cov_total(self, term, th123, th456, geometry=GEOM_SQUARE, thetaMax=0.0, area=0.0, precision=FP64,
-                  cosmo_index=0):
+                  cosmo_index=0, check=True):
         """T1_total / T2_total / T4_total for pairs of triplets
-        (apertureStatisticsCovariance.cu:272-683)."""
+        (apertureStatisticsCovariance.cu:272-683). With check=False an
+        integral that hit its region or sweep cap does not raise; the number of
+        such integrals is left in self.last_capped."""
         a = _arr(th123).reshape(-1, 3)
         b = _arr(th456).reshape(-1, 3)
         out = np.zeros(len(a))
         nb = C.c_int(0)
-        _check(self._h, lib().tp_cov_total_batch(self._h, cosmo_index, term, geometry, thetaMax, area, _dp(a), _dp(b),
-                                                 len(a), precision, _dp(out), C.byref(nb)))
+        rc = lib().tp_cov_total_batch(self._h, cosmo_index, term, geometry, thetaMax, area, _dp(a), _dp(b), len(a),
+                                      precision, _dp(out), C.byref(nb))
+        self.last_capped = nb.value
+        if check or rc != TP_ERR_CAPACITY:
+            _check(self._h, rc)
         return out
 
     def cov_term(self, term, th6, geometry=GEOM_SQUARE, thetaMax=0.0, area=0.0, precision=FP64, cosmo_index=0):
