@@ -7,6 +7,7 @@ torch.utils.cpp_extension: the library is a plain C-ABI shared object.
 from __future__ import annotations
 
 import concurrent.futures as cf
+import json
 import os
 import subprocess
 import sys
@@ -45,7 +46,8 @@ def _deps_mtime():
     for d in (CSRC, CLI, os.path.join(ROOT, "include")):
         for f in os.listdir(d):
             m = max(m, os.path.getmtime(os.path.join(d, f)))
-    return m
+    t = os.path.join(HERE, "tuned.json")
+    return max(m, os.path.getmtime(t)) if os.path.exists(t) else m
 
 
 def _cli_cmds():
@@ -55,12 +57,25 @@ def _cli_cmds():
             for c in CLIS]
 
 
-def build(force: bool = False, verbose: bool = False, extra=()) -> str:
+def tuned_flags():
+    """-D flags of the kernel launch shape chosen by the autotuner (tuned.json)"""
+    try:
+        with open(os.path.join(HERE, "tuned.json")) as f:
+            cfg = json.load(f).get("k_map3", {})
+    except (OSError, ValueError):
+        return []
+    return [f"-D{k}={int(v)}" for k, v in sorted(cfg.items()) if k.startswith("TP_MAP3_")]
+
+
+def build(force: bool = False, verbose: bool = False, extra=(), use_tuned: bool = True) -> str:
     os.makedirs(BIN, exist_ok=True)
     if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= _deps_mtime() and all(
             os.path.exists(os.path.join(BIN, c + ".x")) for c in CLIS):
         return LIB
     nvcc = _nvcc()
+    if use_tuned:
+        given = {e.split("=")[0] for e in extra if e.startswith("-D")}
+        extra = [f for f in tuned_flags() if f.split("=")[0] not in given] + list(extra)
     objs = []
     cmds = []
     for s in sources():
