@@ -469,14 +469,9 @@ __device__ __forceinline__ float2 bispec_pair_node(const float* __restrict__ nf,
   return p2mul(c[NF_W], bispec_pair(c, T, K));
 }
 
-// W B at node j of a pair-interleaved NF_* table, one lane per node
-// (the scalar form of bispec_pair, for callers with one point per lane)
-__device__ __forceinline__ float bispec_node_fast(const float* __restrict__ nf, int j, const TriF& T,
-                                                  const CosmoK<float>& K) {
+// B from one NF_* row c[0..NF_COUNT) (the scalar form of bispec_pair), W not applied
+__device__ __forceinline__ float bispec_fast_row(const float* c, const TriF& T, const CosmoK<float>& K) {
   typedef Mth<float> M;
-  float c[NCP];
-#pragma unroll
-  for (int k = 0; k < NCP; ++k) c[k] = nf[nf_index(j, k)];
   float lq[3], P[3];
 #pragma unroll
   for (int i = 0; i < 3; ++i) lq[i] = T.lg[i] + c[NF_L2S];
@@ -513,7 +508,64 @@ __device__ __forceinline__ float bispec_node_fast(const float* __restrict__ nf, 
     const float e3 = fmaf(en, T.l[0], 1.f) * fmaf(en, T.l[1], 1.f) * fmaf(en, T.l[2], 1.f);
     B = fmaf(2.f * bs3h, M::rcp(e3), bs1h);
   }
-  return c[NF_W] * B;
+  return B;
+}
+
+// W B at node j of a pair-interleaved NF_* table, one lane per node
+__device__ __forceinline__ float bispec_node_fast(const float* __restrict__ nf, int j, const TriF& T,
+                                                  const CosmoK<float>& K) {
+  float c[NCP];
+#pragma unroll
+  for (int k = 0; k < NCP; ++k) c[k] = nf[nf_index(j, k)];
+  return c[NF_W] * bispec_fast_row(c, T, K);
+}
+
+// NF_* row of one arbitrary redshift from its NC_* coefficients zc (zcoefs):
+// the folding of k_node_coefs, for integrands whose redshift varies per point.
+__device__ __forceinline__ void nf_from_nc(const float* zc, float* nf) {
+  typedef Mth<float> M;
+  const float s = zc[NC_S];
+  nf[NF_W] = zc[NC_W];
+  nf[NF_L2S] = zc[NC_L2S];
+  nf[NF_L2HF] = zc[NC_L2HF];
+  nf[NF_HF] = zc[NC_HF];
+  nf[NF_TOFF] = (zc[NC_L2HF] - (float)PLT_LO) * (float)((PLT_N - 1) / (PLT_HI - PLT_LO));
+  nf[NF_ANA] = zc[NC_ANA];
+  nf[NF_L2ANR] = M::lg2(zc[NC_ANR]);
+  nf[NF_ANC] = zc[NC_ANC];
+  nf[NF_L2BN] = M::lg2(zc[NC_BN]);
+  nf[NF_CNS] = zc[NC_CN] * s;
+  nf[NF_ALA] = zc[NC_ALA];
+  nf[NF_ALD] = zc[NC_ALD];
+  nf[NF_BETAB] = zc[NC_BETAB];
+  nf[NF_D1SQ] = zc[NC_D1SQ];
+  nf[NF_D1SQFNS2] = zc[NC_D1SQ] * zc[NC_FN] * s * s;
+  nf[NF_GNS] = zc[NC_GN] * s;
+  nf[NF_HNS2] = zc[NC_HN] * s * s;
+  nf[NF_L2MN] = M::lg2(zc[NC_MN]);
+  nf[NF_L2NN] = M::lg2(zc[NC_NN]);
+  nf[NF_MUN] = zc[NC_MUN];
+  nf[NF_NUN] = zc[NC_NUN];
+  nf[NF_PNS] = zc[NC_PN] * s;
+  nf[NF_ENS] = zc[NC_EN] * s;
+  nf[NF_DNS] = zc[NC_DN] * s;
+  nf[NF_TREE] = zc[NC_TREE];
+  nf[NF_D1P4] = zc[NC_D1P4];
+#pragma unroll
+  for (int k = NF_COUNT; k < NCP; ++k) nf[k] = 0.f;
+}
+
+// the triangle scaled by sc (log2 l2sc): ell_i -> ell_i sc; shape factors unchanged
+__device__ __forceinline__ TriF trif_scaled(const TriF& T, float sc, float l2sc) {
+  TriF S = T;
+  const float sc2 = sc * sc;
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    S.l[i] = T.l[i] * sc;
+    S.l2[i] = T.l2[i] * sc2;
+    S.lg[i] = T.lg[i] + l2sc;
+  }
+  return S;
 }
 
 // Mid-bin two-point interpolation of a z table at fractional bin position fb

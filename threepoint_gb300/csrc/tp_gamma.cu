@@ -14,6 +14,14 @@
 // (point, group) item evaluates 4 Ogata nodes x 3 terms = 12 bispectra.
 #include <cuda_runtime.h>
 
+#include <type_traits>
+
+// resident CTAs per SM requested for the FP32 Gamma kernel (2: <= 128
+// registers per thread; 1: no register cap, one CTA per SM)
+#ifndef TP_GAMMA_MINB
+#define TP_GAMMA_MINB 2
+#endif
+
 #include <cmath>
 #include <complex>
 #include <string>
@@ -107,14 +115,25 @@ struct GammaPolicy {
   static constexpr int G = 8;     // groups of 4 Ogata nodes
   static constexpr int KPG = 4;
   static constexpr int CH = 4;    // regions per chunk (records are large)
-  struct Rec {
-    R zc[NC_COUNT];
-    Tri<R> tri;      // unit-scale triangle (cos psi, sin psi, ell3/psi_k)
-    R invA[3], l2A[3];
-    R cre[3], cim[3];
-    R bmin;
+  // FP64: the per-point NC_* coefficients (bispec_eval); FP32: the folded
+  // NF_* row (bispec_fast_row), an odd number of words (57) per record
+  struct RecD {
+    double zc[NC_COUNT];
+    Tri<double> tri;  // unit-scale triangle (cos psi, sin psi, ell3/psi_k)
+    double invA[3], l2A[3];
+    double cre[3], cim[3];
+    double bmin;
     int live;
   };
+  struct RecF {
+    float nf[NCP];
+    TriF tri;
+    float invA[3], l2A[3];
+    float cre[3], cim[3];
+    float bmin;
+    int live;
+  };
+  typedef typename std::conditional<sizeof(R) == 4, RecF, RecD>::type Rec;
   static constexpr int REC = (int)sizeof(Rec);
   const int* job_order = nullptr;
   static constexpr int PD = 2;
@@ -174,7 +193,13 @@ struct GammaPolicy {
     (void)p;
     Rec& r = *(Rec*)recp;
     const double z = x[0], phi = x[1], psi = x[2];
-    r.live = zcoefs<R>(tab[cosmo], cosm[cosmo], z, r.zc);
+    if constexpr (sizeof(R) == 4) {
+      float zc[NC_COUNT];
+      r.live = zcoefs<float>(tab[cosmo], cosm[cosmo], z, zc);
+      if (r.live) nf_from_nc(zc, r.nf);
+    } else {
+      r.live = zcoefs<R>(tab[cosmo], cosm[cosmo], z, r.zc);
+    }
     if (!r.live) return false;
     // the geometry is evaluated in double: a few dozen operations per point
     // against 96 bispectra
@@ -188,10 +213,13 @@ struct GammaPolicy {
       r.live = 0;
       return false;
     }
-    if constexpr (sizeof(R) == 4)
-      make_tri_phi_f((float)cp, (float)sp, (float)cph, (float)b3, *(Tri<float>*)&r.tri);
-    else
+    if constexpr (sizeof(R) == 4) {
+      Tri<float> t;
+      make_tri_phi_f((float)cp, (float)sp, (float)cph, (float)b3, t);
+      trif_from_tri(t, r.tri);
+    } else {
       make_tri<R>(cp, sp, b3, r.tri);
+    }
     if (which == 0) {
       const double xs[3][2] = {{x1, x2}, {x2, x3}, {x3, x1}};
       for (int j = 0; j < 3; ++j) {
@@ -237,22 +265,42 @@ struct GammaPolicy {
     const CosmoK<R> K = *s_ck;
     const int og = which;
     KSum<R> are, aim;
-    const R* zc = r.zc;
-    const R s = zc[NC_S], l2s = zc[NC_L2S], hf = zc[NC_HF], l2hf = zc[NC_L2HF], W = zc[NC_W];
-    for (int kk = 0; kk < KPG; ++kk) {
-      const int k = 1 + g * KPG + kk;
-      const R psik = (R)c_og.psi[og][k], l2psik = (R)c_og.l2psi[og][k], prodk = (R)c_og.prod[og][k];
+    if constexpr (sizeof(R) == 4) {
+      const float* c = r.nf;
+      const float W = c[NF_W];
+      for (int kk = 0; kk < KPG; ++kk) {
+        const int k = 1 + g * KPG + kk;
+        const float psik = (float)c_og.psi[og][k], l2psik = (float)c_og.l2psi[og][k], prodk = (float)c_og.prod[og][k];
 #pragma unroll
-      for (int j = 0; j < 3; ++j) {
-        R sc = psik * r.invA[j];
-        if (r.bmin * sc <= (R)1.0e-10) continue;  // integrand_bkappa: ell <= 1e-10 -> 0
-        R l2sc = l2psik - r.l2A[j];
-        R B = bispec_eval<R>(zc, 1, s * sc, l2s + l2sc, hf * sc, l2hf + l2sc, r.tri, K);
-        R v = W * B;
-        if (v != v) v = (R)0;  // NaN -> 0 (bispectrum.cu:327-331)
-        v *= prodk;
-        are.add(r.cre[j] * v);
-        aim.add(r.cim[j] * v);
+        for (int j = 0; j < 3; ++j) {
+          const float sc = psik * r.invA[j];
+          if (r.bmin * sc <= 1.0e-10f) continue;  // integrand_bkappa: ell <= 1e-10 -> 0
+          const TriF T = trif_scaled(r.tri, sc, l2psik - r.l2A[j]);
+          float v = W * bispec_fast_row(c, T, K);
+          if (v != v) v = 0.f;  // NaN -> 0 (bispectrum.cu:327-331)
+          v *= prodk;
+          are.add(r.cre[j] * v);
+          aim.add(r.cim[j] * v);
+        }
+      }
+    } else {
+      const R* zc = r.zc;
+      const R s = zc[NC_S], l2s = zc[NC_L2S], hf = zc[NC_HF], l2hf = zc[NC_L2HF], W = zc[NC_W];
+      for (int kk = 0; kk < KPG; ++kk) {
+        const int k = 1 + g * KPG + kk;
+        const R psik = (R)c_og.psi[og][k], l2psik = (R)c_og.l2psi[og][k], prodk = (R)c_og.prod[og][k];
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+          R sc = psik * r.invA[j];
+          if (r.bmin * sc <= (R)1.0e-10) continue;  // integrand_bkappa: ell <= 1e-10 -> 0
+          R l2sc = l2psik - r.l2A[j];
+          R B = bispec_eval<R>(zc, 1, s * sc, l2s + l2sc, hf * sc, l2hf + l2sc, r.tri, K);
+          R v = W * B;
+          if (v != v) v = (R)0;  // NaN -> 0 (bispectrum.cu:327-331)
+          v *= prodk;
+          are.add(r.cre[j] * v);
+          aim.add(r.cim[j] * v);
+        }
       }
     }
     pv[0] = (double)are.s;
@@ -286,7 +334,7 @@ struct GammaPolicy {
 };
 
 template <typename R, int NT>
-__global__ void __launch_bounds__(NT) k_gamma(GammaPolicy<R> pol_in, int njobs, int* job_counter, EngineCfg cfg,
+__global__ void __launch_bounds__(NT, sizeof(R) == 4 ? TP_GAMMA_MINB : 1) k_gamma(GammaPolicy<R> pol_in, int njobs, int* job_counter, EngineCfg cfg,
                                               char* scratch, size_t slot_bytes) {
   GammaPolicy<R> pol = pol_in;
   adaptive_body<3, 2, NT, GammaPolicy<R>>(pol, njobs, job_counter, cfg, scratch, slot_bytes);
