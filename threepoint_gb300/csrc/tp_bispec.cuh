@@ -300,6 +300,13 @@ __device__ __forceinline__ float plin_fast(const CosmoK<float>& K, const float* 
   return plin<float>(K, l * c[NF_HF], lg + c[NF_L2HF]);
 }
 
+// plin<float> kept out of line: the tabulated-P(k) and Eisenstein & Hu
+// branches are not taken when the cubic table exists, and inlined they hold
+// a dozen cosmology constants in registers across the node loops
+__device__ __noinline__ float plin_outline(const CosmoK<float>* K, float kk, float l2kk) {
+  return plin<float>(*K, kk, l2kk);
+}
+
 // ---- packed FP32 pairs (fma/mul/add .f32x2: one issue slot for two lanes) --
 __device__ __forceinline__ float2 p2fma(float2 a, float2 b, float2 c) {
   float2 d;
@@ -443,8 +450,8 @@ __device__ __forceinline__ float2 bispec_pair(const float2* __restrict__ c, cons
         pl = make_float2(r[0], r[1]);
       } else {
         const float2 hf = c[NF_HF], l2hf = c[NF_L2HF];
-        pl.x = plin<float>(K, v2(T.l[i]).x * hf.x, v2(T.lg[i]).x + l2hf.x);
-        pl.y = plin<float>(K, v2(T.l[i]).y * hf.y, v2(T.lg[i]).y + l2hf.y);
+        pl.x = plin_outline(&K, v2(T.l[i]).x * hf.x, v2(T.lg[i]).x + l2hf.x);
+        pl.y = plin_outline(&K, v2(T.l[i]).y * hf.y, v2(T.lg[i]).y + l2hf.y);
       }
     }
     const float2 a = p2mul(p2mul(num, p2rcp(den)), pl);

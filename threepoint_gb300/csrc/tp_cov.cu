@@ -16,6 +16,8 @@
 // splits them into (P index x node group) items.
 #include <cuda_runtime.h>
 
+#include <type_traits>
+
 #include <algorithm>
 #include <array>
 #include <cmath>
@@ -250,17 +252,25 @@ struct BkProd {
   static constexpr int NS = 2;
   __device__ static int slot(int g) { return g >> 3; }
   static constexpr int CH = 4;
-  struct Rec {
-    Tri<R> t[2];
+  // FP64 rows NC_* with Tri<double>; FP32 rows NF_* (pair-interleaved, packed
+  // node pairs as in k_map3) with TriF
+  struct RecD {
+    Tri<double> t[2];
     double wt;
     int valid;
   };
+  struct RecF {
+    TriF t[2];
+    double wt;
+    int valid;
+  };
+  typedef typename std::conditional<sizeof(R) == 4, RecF, RecD>::type Rec;
   static constexpr int REC = (int)sizeof(Rec);
   const int* job_order = nullptr;
   static constexpr size_t PSMEM = sizeof(R) * NCP * NNODE + sizeof(CosmoK<R>) + 64;
 
   const CovJob* jobs;
-  const R* ncoef;
+  const R* ncoef;  // NC_* rows (FP64) or NF_* rows (FP32) of the cosmology
   double wscale;
   CosmoK<R> ck;
   double norm;
@@ -310,8 +320,16 @@ struct BkProd {
     r.valid = !zero && wt != 0.0;
     r.wt = wt;
     if (r.valid) {
-      make_tri<R>(l1, l2, l3, r.t[0]);
-      make_tri<R>(l1, l5, l6, r.t[1]);
+      if constexpr (sizeof(R) == 4) {
+        Tri<float> t;
+        make_tri<float>(l1, l2, l3, t);
+        trif_from_tri(t, r.t[0]);
+        make_tri<float>(l1, l5, l6, t);
+        trif_from_tri(t, r.t[1]);
+      } else {
+        make_tri<R>(l1, l2, l3, r.t[0]);
+        make_tri<R>(l1, l5, l6, r.t[1]);
+      }
     }
     return r.valid;
   }
@@ -319,15 +337,30 @@ struct BkProd {
   __device__ void group(const char* recp, int g, double* pv) {
     const Rec& r = *(const Rec*)recp;
     const int i = g >> 3, ch = g & 7;
-    KSum<R> acc;
     const int j0 = ch * 12;
+    if constexpr (sizeof(R) == 4) {
+      // two nodes per step in packed FP32 pairs; Kahan sum per lane
+      float2 sm = make_float2(0.f, 0.f), cmp = make_float2(0.f, 0.f);
+      for (int p = j0 / 2; p < (j0 + 12) / 2; ++p) {
+        float2 v = bispec_pair_node(s_nc, p, r.t[i], ck);
+        if (v.x != v.x) v.x = 0.f;
+        if (v.y != v.y) v.y = 0.f;
+        const float2 y = p2sub(v, cmp);
+        const float2 t = p2add(sm, y);
+        cmp = p2sub(p2sub(t, sm), y);
+        sm = t;
+      }
+      pv[0] = (double)sm.x + (double)sm.y;
+    } else {
+      KSum<R> acc;
 #pragma unroll 2
-    for (int j = j0; j < j0 + 12; ++j) {
-      R v = bispec_node<R>(s_nc, j, r.t[i], ck);
-      if (v != v) v = (R)0;
-      acc.add(v);
+      for (int j = j0; j < j0 + 12; ++j) {
+        R v = bispec_node<R>(s_nc, j, r.t[i], ck);
+        if (v != v) v = (R)0;
+        acc.add(v);
+      }
+      pv[0] = (double)acc.s;
     }
-    pv[0] = (double)acc.s;
   }
 
   __device__ void finalize(const char* recp, const double* sum, double* fv) {
@@ -565,7 +598,7 @@ static int run_t4(tp_ctx* ctx, int cosmo, const JobSet& js, double norm, std::ve
   BkProd<R> pol;
   memset(&pol, 0, sizeof(pol));
   pol.jobs = (const CovJob*)(b + o_j);
-  pol.ncoef = (sizeof(R) == 8 ? (const R*)(const void*)ctx->d_ncoef64 : (const R*)(const void*)ctx->d_ncoef32) +
+  pol.ncoef = (sizeof(R) == 8 ? (const R*)(const void*)ctx->d_ncoef64 : (const R*)(const void*)ctx->d_fcoef32) +
               (size_t)cosmo * NCP * NNODE;
   CosmoK<R> ck;
   double ws = 1.0;

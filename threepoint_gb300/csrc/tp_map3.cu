@@ -191,7 +191,7 @@ struct Map3Policy {
   // line-of-sight partial sum over node group g (only called for live points)
   __device__ void group(const char* recp, int g, double* pv) {
     const Rec& r = *(const Rec*)recp;
-    const CosmoK<R> K = *s_ck;
+    const CosmoK<R>& K = *s_ck;  // fields read from shared memory where used
     const int j0 = g * NPG;
     if constexpr (sizeof(R) == 4) {
       // two nodes per step in packed FP32 pairs; Kahan sum per lane
