@@ -303,7 +303,7 @@ __device__ __forceinline__ float plin_fast(const CosmoK<float>& K, const float* 
 // plin<float> kept out of line: the tabulated-P(k) and Eisenstein & Hu
 // branches are not taken when the cubic table exists, and inlined they hold
 // a dozen cosmology constants in registers across the node loops
-__device__ __noinline__ float plin_outline(const CosmoK<float>* K, float kk, float l2kk) {
+static __device__ __noinline__ float plin_outline(const CosmoK<float>* K, float kk, float l2kk) {
   return plin<float>(*K, kk, l2kk);
 }
 
