@@ -369,12 +369,18 @@ class Context:
         return lib().tp_ctx_stream(self._h)
 
     # -- shear 3PCF (cuda_version/gamma.cu:98-148) ---------------------------
-    def gamma_batch(self, x, comp_mask=0xF, rel_tol=1e-3, precision=FP64, cosmo_index=0):
+    def gamma_batch(self, x, comp_mask=0xF, rel_tol=1e-3, precision=FP64, cosmo_index=0, check=True):
+        """With check=False, triangles whose integrals hit a region or sweep
+        cap do not raise; their per-triangle status is left in
+        self.last_gamma_status (0 = converged)."""
         x = _arr(x).reshape(-1, 3)
         out = np.zeros(len(x) * 8)
         st = np.zeros(len(x), dtype=np.int32)
-        _check(self._h, lib().tp_gamma_batch(self._h, cosmo_index, _dp(x), len(x), comp_mask, rel_tol, precision,
-                                             _dp(out), st.ctypes.data_as(C.POINTER(C.c_int))))
+        rc = lib().tp_gamma_batch(self._h, cosmo_index, _dp(x), len(x), comp_mask, rel_tol, precision, _dp(out),
+                                  st.ctypes.data_as(C.POINTER(C.c_int)))
+        self.last_gamma_status = st
+        if check or rc != TP_ERR_CAPACITY:
+            _check(self._h, rc)
         o = out.reshape(-1, 4, 2)
         return o[..., 0] + 1j * o[..., 1]
 
