@@ -7,6 +7,8 @@
 // type: double is the plain FP64 path; float uses the SFU approximations
 // ex2/lg2/rcp.approx and is summed with Kahan compensation by its callers.
 #pragma once
+#include <type_traits>
+
 #include "tp_internal.cuh"
 
 namespace tp {
@@ -46,6 +48,11 @@ struct CosmoK {
   R h;
   int pk_given;
   R ln_kmin, inv_dk;  // tabulated P(k)
+  // log2(ell) range for which every fixed line-of-sight node's P(k) table
+  // coordinate lies inside the table (set with the node table; the packed
+  // node-pair path clamps log2(ell) into it once per point instead of
+  // clamping the coordinate at every node)
+  R lgp_lo, lgp_hi;
   const double* pk;   // 256 values (FP64, read through the cache)
   const float* plt;   // log2 P_lin cubic segments (PLT_N float4) for the FP32 path, or null
 };
@@ -70,6 +77,8 @@ __host__ __device__ inline CosmoK<R> make_cosmok(const EHConst& e, const CosmoDe
   k.inv_dk = (R)(c.pk_given ? 1.0 / c.dk : 0.0);
   k.pk = pk_dev;
   k.plt = nullptr;
+  k.lgp_lo = (R)-1e30;
+  k.lgp_hi = (R)1e30;
   return k;
 }
 
@@ -353,8 +362,11 @@ struct TriF2 {
   float2 l[3], lg[3], l2[3];
   float2 log2r1, r2sq, pr2;
   float2 f2t[3];
+  float2 lgp[3];  // log2 ell_i clamped into [lgp_lo, lgp_hi] (P(k) table lookups only)
 };
-__device__ __forceinline__ void trif2_from(const TriF& T, TriF2& D) {
+__device__ __forceinline__ void trif2_from(const TriF& T, TriF2& D, float lgp_lo, float lgp_hi) {
+#pragma unroll
+  for (int i = 0; i < 3; ++i) D.lgp[i] = p2dup(fminf(fmaxf(T.lg[i], lgp_lo), lgp_hi));
 #pragma unroll
   for (int i = 0; i < 3; ++i) {
     D.l[i] = p2dup(T.l[i]);
@@ -435,12 +447,17 @@ __device__ __forceinline__ float2 bispec_pair(const float2* __restrict__ c, cons
     float2 pl;
     {
       constexpr float INV = (float)((PLT_N - 1) / (PLT_HI - PLT_LO));
-      const float2 t2 = p2fma(v2(T.lg[i]), p2dup(INV), c[NF_TOFF]);
+      constexpr bool pre = std::is_same<TT, TriF2>::value;  // log2 ell already clamped per point
+      float2 t2;
+      if constexpr (pre)
+        t2 = p2fma(T.lgp[i], p2dup(INV), c[NF_TOFF]);
+      else
+        t2 = p2fma(v2(T.lg[i]), p2dup(INV), c[NF_TOFF]);
       if (K.plt) {
         float tt[2] = {t2.x, t2.y}, r[2];
 #pragma unroll
         for (int h = 0; h < 2; ++h) {
-          const float t = fminf(fmaxf(tt[h], 0.f), (float)(PLT_N - 1) - 1e-3f);
+          const float t = pre ? tt[h] : fminf(fmaxf(tt[h], 0.f), (float)(PLT_N - 1) - 1e-3f);
           const float tm = __fadd_rd(t, 12582912.f);  // 1.5 * 2^23 + floor(t)
           const int ix = __float_as_int(tm) - 0x4B400000;
           const float f = t - (tm - 12582912.f);

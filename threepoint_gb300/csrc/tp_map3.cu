@@ -199,7 +199,7 @@ struct Map3Policy {
       const TriF& T2 = r.tri;  // pairs formed where used
 #else
       TriF2 T2;  // pairs held in registers across the node loop
-      trif2_from(r.tri, T2);
+      trif2_from(r.tri, T2, K.lgp_lo, K.lgp_hi);
 #endif
       float2 s = make_float2(0.f, 0.f), cmp = make_float2(0.f, 0.f);
       TP_UNROLL(TP_MAP3_UNROLL)

@@ -522,7 +522,19 @@ __global__ void k_finish(const CosmoDev* cos, const EHConst* eh, const TablesDev
     wscale64[ci] = 1.0;
     wscale32[ci] = wmax;
     ck64[ci] = make_cosmok<double>(eh[ci], cos[ci], tab[ci].pk);
-    ck32[ci] = make_cosmok<float>(eh[ci], cos[ci], tab[ci].pk);
+    CosmoK<float> k32 = make_cosmok<float>(eh[ci], cos[ci], tab[ci].pk);
+    // log2(ell) range keeping every node's table coordinate
+    // (log2 ell + log2(h/f_K) - PLT_LO) * INV at least 0.05 octaves (~1 cell)
+    // inside the table
+    double lo = -1e300, hi = 1e300;
+    for (int j = 0; j < NNODE; ++j) {
+      const double l2hf = ncoef[((size_t)ci * NNODE + j) * NCP + NC_L2HF];
+      lo = fmax(lo, PLT_LO - l2hf + 0.05);
+      hi = fmin(hi, PLT_HI - l2hf - 0.05);
+    }
+    k32.lgp_lo = (float)lo;
+    k32.lgp_hi = (float)hi;
+    ck32[ci] = k32;
   }
   __syncthreads();
   for (int j = threadIdx.x; j < NNODE; j += blockDim.x) {
