@@ -45,6 +45,7 @@ struct TablesDev {
   double f_K[NZ], g[NZ], D1[NZ], r_sigma[NZ], n_eff[NZ], ncur[NZ];
   double pk[NK];
   double norm, dz;
+  double lgr0;  // growth integral at z = 0 (D1 = lgr(z) / lgr0)
 };
 
 // Per-node BiHalofit coefficients for the fixed line-of-sight nodes of

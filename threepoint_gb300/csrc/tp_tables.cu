@@ -237,7 +237,13 @@ __device__ double d_lgr(const CosmoDev& c, double z) {
 // kernels
 // ---------------------------------------------------------------------------
 
-// norm = sigma8 / sigma(8 Mpc/h, top hat); one warp per cosmology
+// The table kernels run as one-warp blocks: a block needs at most 128 x 32
+// registers and a few KB of shared memory, so it fits beside three resident
+// k_map3 CTAs and the next batch's tables build on the FP64 pipe while the
+// current batch integrates.
+
+// norm = sigma8 / sigma(8 Mpc/h, top hat) and the growth integral at z = 0;
+// one warp per cosmology
 __global__ void k_norm(const CosmoDev* cos, EHConst* eh, TablesDev* tab, int n) {
   int ci = blockIdx.x;
   if (ci >= n) return;
@@ -249,47 +255,45 @@ __global__ void k_norm(const CosmoDev* cos, EHConst* eh, TablesDev* tab, int n) 
     tab[ci].norm = norm;
     tab[ci].dz = c.zmax / NZ;
     eh[ci].ehc = e.ehc * norm * norm;
+    tab[ci].lgr0 = d_lgr(c, 0.);
   }
 }
 
-// f_K on bin centres and lensing efficiency g (bispectrum.cu:158-190)
-__global__ void k_fk_g(const CosmoDev* cos, const double* nz, int nz_stride, TablesDev* tab, int n) {
-  int ci = blockIdx.x;
+// f_K on bin centres (bispectrum.cu:158-166); block b of a cosmology takes
+// bins 32 b .. 32 b + 31
+__global__ void k_fk(const CosmoDev* cos, TablesDev* tab, int n) {
+  const int ci = blockIdx.x / (NZ / 32), i = (blockIdx.x % (NZ / 32)) * 32 + threadIdx.x;
   if (ci >= n) return;
   const CosmoDev c = cos[ci];
-  TablesDev& t = tab[ci];
   const double dz = c.zmax / NZ;
-  __shared__ double fk[NZ];
-  for (int i = threadIdx.x; i < NZ; i += blockDim.x) {
-    double zb = (i + 0.5) * dz;
-    double cx = zb / 2, dx = zb / 2, q = 0;
-    for (int m = 0; m < 48; m++) q += c_gq_w[m] * (1. / d_E(c, cx - dx * c_gq_a[m]) + 1. / d_E(c, cx + dx * c_gq_a[m]));
-    fk[i] = C_OVER_H0 * (q * dx);
-    t.f_K[i] = fk[i];
-  }
-  __syncthreads();
+  double zb = (i + 0.5) * dz;
+  double cx = zb / 2, dx = zb / 2, q = 0;
+  for (int m = 0; m < 48; m++) q += c_gq_w[m] * (1. / d_E(c, cx - dx * c_gq_a[m]) + 1. / d_E(c, cx + dx * c_gq_a[m]));
+  tab[ci].f_K[i] = C_OVER_H0 * (q * dx);
+}
+
+// lensing efficiency g by the trapezoid sum over n(z) (bispectrum.cu:168-190)
+__global__ void k_g(const CosmoDev* cos, const double* nz, int nz_stride, TablesDev* tab, int n) {
+  const int ci = blockIdx.x / (NZ / 32), i = (blockIdx.x % (NZ / 32)) * 32 + threadIdx.x;
+  if (ci >= n) return;
+  const double dz = cos[ci].zmax / NZ;
+  TablesDev& t = tab[ci];
+  const double* fk = t.f_K;
   const double* nzc = nz + (size_t)ci * nz_stride;
-  for (int i = threadIdx.x; i < NZ; i += blockDim.x) {
-    double gi = 0;
-    for (int j = i; j < NZ; j++) {
-      double term = nzc[j] * (fk[j] - fk[i]) / fk[j];
-      gi += (j == i || j == NZ - 1) ? term / 2 : term;
-    }
-    t.g[i] = (i == 0) ? 1.0 : gi * dz;
+  double gi = 0;
+  for (int j = i; j < NZ; j++) {
+    double term = nzc[j] * (fk[j] - fk[i]) / fk[j];
+    gi += (j == i || j == NZ - 1) ? term / 2 : term;
   }
+  t.g[i] = (i == 0) ? 1.0 : gi * dz;
 }
 
 // linear growth D1 = lgr(z)/lgr(0) on bin centres (bispectrum.cu:207)
 __global__ void k_growth(const CosmoDev* cos, TablesDev* tab, int n) {
-  int ci = blockIdx.x;
+  const int ci = blockIdx.x / (NZ / 32), i = (blockIdx.x % (NZ / 32)) * 32 + threadIdx.x;
   if (ci >= n) return;
   const CosmoDev c = cos[ci];
-  __shared__ double lgr0;
-  if (threadIdx.x == NZ) lgr0 = d_lgr(c, 0.);
-  double v = 0;
-  if (threadIdx.x < NZ) v = d_lgr(c, (threadIdx.x + 0.5) * (c.zmax / NZ));
-  __syncthreads();
-  if (threadIdx.x < NZ) tab[ci].D1[threadIdx.x] = v / lgr0;
+  tab[ci].D1[i] = d_lgr(c, (i + 0.5) * (c.zmax / NZ)) / tab[ci].lgr0;
 }
 
 // r_sigma by bisection on D1 sigma(1/k) = 1, then n_eff and ncur
@@ -372,8 +376,9 @@ __device__ inline double interp_mid(const double* arr, double zfrac_bins) {
 // (limber_integrand_power_spectrum + P_k_nonlinear, bispectrum.cu:531-600,951-991).
 __global__ void k_node_coefs(const CosmoDev* cos, const TablesDev* tab, double* ncoef, float* ncoef_f, float* fcoef_f,
                              double* hcoef, float* hcoef_f, int n) {
-  int ci = blockIdx.x;
-  int j = threadIdx.x;
+  // one warp per 32 nodes of a cosmology
+  int ci = blockIdx.x / (NNODE / 32);
+  int j = (blockIdx.x % (NNODE / 32)) * 32 + threadIdx.x;
   if (ci >= n || j >= NNODE) return;
   const CosmoDev c = cos[ci];
   const TablesDev& t = tab[ci];
@@ -547,18 +552,25 @@ __global__ void k_finish(const CosmoDev* cos, const EHConst* eh, const TablesDev
 // log2 P_lin on the FP32 interpolation grid (log2(k h) uniform on [PLT_LO, PLT_HI])
 // and its Catmull-Rom cubic per interval i: y(i + f) = y0 + f (c1 + f (c2 + f c3))
 __global__ void k_plin_table(const CosmoDev* cos, const EHConst* eh, float4* plt, CosmoK<float>* ck32, int n) {
-  int ci = blockIdx.x;
+  // block b of a cosmology builds intervals [b * PLT_SLICE, (b + 1) * PLT_SLICE)
+  constexpr int PLT_SLICE = 128;
+  const int ci = blockIdx.x / (PLT_N / PLT_SLICE), a = (blockIdx.x % (PLT_N / PLT_SLICE)) * PLT_SLICE;
   if (ci >= n) return;
   const CosmoDev c = cos[ci];
   const EHConst e = eh[ci];
-  __shared__ double y[PLT_N + 2];
-  for (int i = threadIdx.x; i < PLT_N + 2; i += blockDim.x) {
-    double kk = exp2(PLT_LO + (i - 1) * (PLT_HI - PLT_LO) / (PLT_N - 1));
-    y[i] = log2(eh_linear_pk(e, kk / c.h));
+  // y[m] = log2 P at grid point m - 1, m = 0 .. PLT_N + 1; this slice needs
+  // y[a .. a + PLT_SLICE + 3]
+  __shared__ double y[PLT_SLICE + 4];
+  for (int k = threadIdx.x; k < PLT_SLICE + 4; k += blockDim.x) {
+    const int m = a + k;
+    if (m > PLT_N + 1) continue;
+    double kk = exp2(PLT_LO + (m - 1) * (PLT_HI - PLT_LO) / (PLT_N - 1));
+    y[k] = log2(eh_linear_pk(e, kk / c.h));
   }
   __syncthreads();
-  for (int i = threadIdx.x; i < PLT_N; i += blockDim.x) {
-    double ym1 = y[i], y0 = y[i + 1], y1 = y[i + 2], y2 = i + 3 < PLT_N + 2 ? y[i + 3] : y[i + 2];
+  for (int u = threadIdx.x; u < PLT_SLICE; u += blockDim.x) {
+    const int i = a + u;
+    double ym1 = y[u], y0 = y[u + 1], y1 = y[u + 2], y2 = i + 3 < PLT_N + 2 ? y[u + 3] : y[u + 2];
     float4 q;
     q.x = (float)y0;
     q.y = (float)(0.5 * (y1 - ym1));
@@ -566,7 +578,7 @@ __global__ void k_plin_table(const CosmoDev* cos, const EHConst* eh, float4* plt
     q.w = (float)(0.5 * (3 * (y0 - y1) + y2 - ym1));
     plt[(size_t)ci * PLT_N + i] = q;
   }
-  if (threadIdx.x == 0 && !c.pk_given) ck32[ci].plt = (const float*)(plt + (size_t)ci * PLT_N);
+  if (a == 0 && threadIdx.x == 0 && !c.pk_given) ck32[ci].plt = (const float*)(plt + (size_t)ci * PLT_N);
 }
 
 // ---------------------------------------------------------------------------
@@ -582,16 +594,16 @@ cudaError_t build_tables(const CosmoDev* d_cos, EHConst* d_eh, const double* d_n
                          double* d_wscale64,
                          double* d_wscale32, CosmoK<double>* d_ck64, CosmoK<float>* d_ck32, float4* d_plt, int n,
                          cudaStream_t s) {
+  // every launch is made of one-warp blocks (see above)
   k_norm<<<n, 32, 0, s>>>(d_cos, d_eh, d_tab, n);
-  k_fk_g<<<n, 256, 0, s>>>(d_cos, d_nz, nz_stride, d_tab, n);
-  k_growth<<<n, NZ + 32, 0, s>>>(d_cos, d_tab, n);
-  long warps = (long)n * NZ;
-  int wpb = 4;
-  k_rsigma<<<(unsigned)((warps + wpb - 1) / wpb), 32 * wpb, 0, s>>>(d_cos, d_eh, d_tab, n);
-  k_node_coefs<<<n, NNODE, 0, s>>>(d_cos, d_tab, d_ncoef, d_ncoef_f, d_fcoef_f, d_hcoef, d_hcoef_f, n);
-  k_finish<<<n, NNODE, 0, s>>>(d_cos, d_eh, d_tab, d_ncoef, d_ncoef_f, d_fcoef_f, d_wscale64, d_wscale32, d_ck64, d_ck32,
-                               n);
-  k_plin_table<<<n, 256, 0, s>>>(d_cos, d_eh, d_plt, d_ck32, n);
+  k_fk<<<n * (NZ / 32), 32, 0, s>>>(d_cos, d_tab, n);
+  k_g<<<n * (NZ / 32), 32, 0, s>>>(d_cos, d_nz, nz_stride, d_tab, n);
+  k_growth<<<n * (NZ / 32), 32, 0, s>>>(d_cos, d_tab, n);
+  k_rsigma<<<(unsigned)((long)n * NZ), 32, 0, s>>>(d_cos, d_eh, d_tab, n);
+  k_node_coefs<<<n * (NNODE / 32), 32, 0, s>>>(d_cos, d_tab, d_ncoef, d_ncoef_f, d_fcoef_f, d_hcoef, d_hcoef_f, n);
+  k_finish<<<n, 32, 0, s>>>(d_cos, d_eh, d_tab, d_ncoef, d_ncoef_f, d_fcoef_f, d_wscale64, d_wscale32, d_ck64, d_ck32,
+                            n);
+  k_plin_table<<<n * (PLT_N / 128), 32, 0, s>>>(d_cos, d_eh, d_plt, d_ck32, n);
   return cudaGetLastError();
 }
 
