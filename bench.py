@@ -200,10 +200,10 @@ def run_ours(args):
         batch = cosmo_batch(step)
         ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
         with torch.cuda.stream(st):
-            if flush_first:
-                flush.zero_()  # L2 flush between steps (on this step's stream)
             ev[0].record(st)
             c.set_cosmologies(batch, nz)
+            if flush_first:
+                flush.zero_()  # L2 flush before the step's integrals (on this step's stream)
             ev[1].record(st)
             c.map3_jobs_device(job_cosmo, job_theta, b["out"], b["err"], b["nev"], b["status"], lMax=lmax,
                                rel_tol=1e-4, precision=tp.FP32, nlive=b["nlive"], job_order=order[0])
@@ -261,9 +261,8 @@ def run_ours(args):
     live_total = 0
     n_roof = min(args.steps, 3)
     for s in range(n_roof):
-        flush.zero_()
         torch.cuda.synchronize()
-        one_step(args.warmup + s, 0, timings)
+        one_step(args.warmup + s, 0, timings, flush_first=True)
         torch.cuda.synchronize()
         live_total += int(nlive.sum().item())
         if args.dump_costs and s == 0:

@@ -594,7 +594,20 @@ cudaError_t build_tables(const CosmoDev* d_cos, EHConst* d_eh, const double* d_n
                          double* d_wscale64,
                          double* d_wscale32, CosmoK<double>* d_ck64, CosmoK<float>* d_ck32, float4* d_plt, int n,
                          cudaStream_t s) {
-  // every launch is made of one-warp blocks (see above)
+  // every launch is made of one-warp blocks (see above). An SM runs blocks of
+  // different kernels together only in one shared-memory/L1 configuration:
+  // these kernels ask for the one k_map3 runs in (maximum shared memory).
+  static thread_local int carveout_set = -1;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (carveout_set != dev) {
+    const void* ks[] = {(const void*)k_norm, (const void*)k_fk, (const void*)k_g, (const void*)k_growth,
+                        (const void*)k_rsigma, (const void*)k_node_coefs, (const void*)k_finish,
+                        (const void*)k_plin_table};
+    for (const void* k : ks)
+      cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
+    carveout_set = dev;
+  }
   k_norm<<<n, 32, 0, s>>>(d_cos, d_eh, d_tab, n);
   k_fk<<<n * (NZ / 32), 32, 0, s>>>(d_cos, d_tab, n);
   k_g<<<n * (NZ / 32), 32, 0, s>>>(d_cos, d_nz, nz_stride, d_tab, n);
