@@ -38,9 +38,9 @@ LHS_SEED = 20261203
 N_LHS = 4096
 # DRAM bytes (read + write) of one k_map3<float> launch per integral, from
 # ncu dram__bytes_read.sum + dram__bytes_write.sum of a 880-integral launch
-# (4 LHS cosmologies x 220 triplets: 71.2 + 228.3 MB); the region-store
+# (4 LHS cosmologies x 220 triplets: 65.9 + 221.5 MB); the region-store
 # traffic grows with the number of integrals
-TRAFFIC_PER_INTEGRAL = (71.241984e6 + 228.270848e6) / 880
+TRAFFIC_PER_INTEGRAL = (65.906176e6 + 221.541888e6) / 880
 SFU_PER_NODE = 27  # SFU ops (ex2/rcp.approx) per line-of-sight node of the FP32 BiHalofit evaluation (NF_* rows)
 NNODE = 96
 
