@@ -129,3 +129,30 @@ def test_invalid_arguments_raise(gpu_ctx):
         gpu_ctx.map3_batch([[1e-3, 1e-3, 1e-3]], cosmo_index=[5])
     with pytest.raises(tp.ThreepointError):
         gpu_ctx.bkappa([[1.0, 1.0, 1.0]], cosmo_index=[3])
+
+
+def test_region_cap_exhaustion_reports_and_recovers(nz256):
+    """A forced region-cap exhaustion: the call reports TP_ERR_CAPACITY with
+    the per-integral status and still writes the value; the context stays
+    usable and the same integral converges once the cap allows it."""
+    import threepoint_gb300 as tp
+
+    arc = 2.9088820866e-4
+    th = [[1 * arc, 1 * arc, 1 * arc]]
+    ctx = tp.Context(0)
+    with pytest.raises(tp.ThreepointError):
+        ctx.set_limits(region_cap=63)
+    ctx.set_cosmology(tp.cosmology(**COSMO1), nz256)
+    ctx.set_limits(region_cap=64)
+    with pytest.raises(tp.ThreepointError) as e:
+        ctx.map3_batch(th, precision=tp.FP32)
+    assert e.value.status == tp.TP_ERR_CAPACITY
+    v, info = ctx.map3_batch(th, precision=tp.FP32, return_info=True, check=False)
+    assert info["status"][0, 0] & 1  # region cap
+    assert np.isfinite(v).all()
+    ctx.set_limits(region_cap=32768)
+    v2, info2 = ctx.map3_batch(th, precision=tp.FP32, return_info=True)
+    assert info2["status"][0, 0] == 0
+    ref = ctx.map3_batch(th, precision=tp.FP64)
+    assert v2[0, 0] == pytest.approx(ref[0, 0], rel=1e-3)
+    ctx.close()
