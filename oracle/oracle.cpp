@@ -1067,23 +1067,31 @@ double psip_fn(double t) {
   double den = cosh(PI * sinh(t)) + 1;
   return num / den;
 }
-constexpr int PREC_K = 33;     // int(3.31/0.1), gamma.cuh:29-30
-constexpr double PREC_H = 0.1;
+// Ogata step and node count: the CUDA values by default (gamma.cuh:29-30:
+// prec_h = 0.1, prec_k = int(3.31 / 0.1)); orc_set_ogata changes them (the
+// classed test of the analytic bispectrum uses h = 0.01, k up to 3.5).
+double g_prec_h = 0.1;
+int g_prec_k = 33;
 
 struct Ogata {
-  double psi6[PREC_K], prod6[PREC_K], psi2[PREC_K], prod2[PREC_K];
-  Ogata() {
+  double h = 0;
+  int nk = 0;
+  std::vector<double> psi6, prod6, psi2, prod2;
+  void build(double hh, int n) {
+    h = hh;
+    nk = n;
+    psi6.assign(n, 0), prod6.assign(n, 0), psi2.assign(n, 0), prod2.assign(n, 0);
     // compute_weights_bessel, gamma.cu:13-56
     for (int pass = 0; pass < 2; ++pass) {
       int nu = pass == 0 ? 6 : 2;
-      double* ps = pass == 0 ? psi6 : psi2;
-      double* pr = pass == 0 ? prod6 : prod2;
-      for (int i = 0; i < PREC_K; ++i) {
+      double* ps = pass == 0 ? psi6.data() : psi2.data();
+      double* pr = pass == 0 ? prod6.data() : prod2.data();
+      for (int i = 0; i < n; ++i) {
         double z = bessel_zero(nu, i);
         double pz = z / PI;
-        ps[i] = PI * psi_fn(pz * PREC_H) / PREC_H;
+        ps[i] = PI * psi_fn(pz * h) / h;
         double Jb = std::cyl_bessel_j((double)nu, ps[i]);
-        double pp = psip_fn(PREC_H * pz);
+        double pp = psip_fn(h * pz);
         double Jn1 = i == 0 ? 0.0 : std::cyl_bessel_j((double)nu + 1, z);
         double w = 2 / (PI * z * pow(Jn1, 2));
         pr[i] = w * pow(ps[i], 3) * Jb * pp;
@@ -1093,6 +1101,7 @@ struct Ogata {
 };
 const Ogata& ogata() {
   static Ogata o;
+  if (o.h != g_prec_h || o.nk != g_prec_k) o.build(g_prec_h, g_prec_k);
   return o;
 }
 
@@ -1170,15 +1179,24 @@ int integrand_gamma_v(unsigned ndim, size_t npts, const double* x, void* fdata, 
 #pragma omp parallel for schedule(dynamic, 4) if (npts > 64)
   for (long i = 0; i < (long)npts; ++i) {
     double z = x[i * 3], phi = x[i * 3 + 1], psi = x[i * 3 + 2];
-    // pairwise tree over k=1..32 as the shared-memory reduction (gamma.cu:291-305)
-    cplx v[32];
-    for (int k = 1; k < PREC_K; ++k)
-      v[k - 1] = g->which == 0 ? full_integrand_gamma0(g->t, phi, psi, z, k, g->x1, g->x2, g->x3)
-                               : full_integrand_gamma1(g->t, phi, psi, z, k, g->x1, g->x2, g->x3);
-    for (int size = 16; size > 0; size /= 2)
-      for (int j = 0; j < size; ++j) v[j] += v[j + size];
-    fval[2 * i] = v[0].real();
-    fval[2 * i + 1] = v[0].imag();
+    const int nk = ogata().nk;
+    cplx s0(0, 0);
+    if (nk == 33) {
+      // pairwise tree over k=1..32 as the shared-memory reduction (gamma.cu:291-305)
+      cplx v[32];
+      for (int k = 1; k < nk; ++k)
+        v[k - 1] = g->which == 0 ? full_integrand_gamma0(g->t, phi, psi, z, k, g->x1, g->x2, g->x3)
+                                 : full_integrand_gamma1(g->t, phi, psi, z, k, g->x1, g->x2, g->x3);
+      for (int size = 16; size > 0; size /= 2)
+        for (int j = 0; j < size; ++j) v[j] += v[j + size];
+      s0 = v[0];
+    } else {
+      for (int k = 1; k < nk; ++k)
+        s0 += g->which == 0 ? full_integrand_gamma0(g->t, phi, psi, z, k, g->x1, g->x2, g->x3)
+                            : full_integrand_gamma1(g->t, phi, psi, z, k, g->x1, g->x2, g->x3);
+    }
+    fval[2 * i] = s0.real();
+    fval[2 * i + 1] = s0.imag();
   }
   return 0;
 }
@@ -1204,19 +1222,27 @@ cplx orthocenter_to_centroid(cplx g, double x1, double x2, double x3, bool conj1
 
 }  // namespace
 
+extern "C" void orc_set_ogata(double h, int nk) {
+  g_prec_h = h;
+  g_prec_k = nk;
+  (void)ogata();  // build now, outside any parallel region
+}
+
 extern "C" void orc_ogata_weights(double* out) {
   const Ogata& O = ogata();
-  for (int k = 0; k < PREC_K; ++k) {
+  const int n = O.nk;
+  for (int k = 0; k < n; ++k) {
     out[k] = O.psi6[k];
-    out[PREC_K + k] = O.prod6[k];
-    out[2 * PREC_K + k] = O.psi2[k];
-    out[3 * PREC_K + k] = O.prod2[k];
+    out[n + k] = O.prod6[k];
+    out[2 * n + k] = O.psi2[k];
+    out[3 * n + k] = O.prod2[k];
   }
 }
 
 // gamma0..gamma3, gamma.cu:98-148
 extern "C" void orc_gamma(const orc_tables* t, int comp, double x1, double x2, double x3, double relTol,
                           double absTol, double* re, double* im, long* neval) {
+  (void)ogata();  // the node table is built on the calling thread
   if (comp == 2) {  // gamma2 = gamma1(x2,x3,x1)
     orc_gamma(t, 1, x2, x3, x1, relTol, absTol, re, im, neval);
     return;

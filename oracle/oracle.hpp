@@ -88,6 +88,8 @@ void orc_gamma(const orc_tables* t, int comp, double x1, double x2, double x3,
 // closed-form Gamma^0 of the analytic test bispectrum
 // (classed_version/gamma.cpp:83-93,567-582)
 void orc_ggg_analytic(double r1, double r2, double r3, double* re, double* im);
+// Ogata step h and node count (default 0.1 and 33, the CUDA settings)
+void orc_set_ogata(double h, int nk);
 
 // ---- <Map^3> covariance (cuda_version/apertureStatisticsCovariance.cu) ----
 typedef struct {

@@ -126,3 +126,37 @@ def test_ogata_nodes_against_scipy_zeros():
         # psi_k approaches the zeros of J_nu as k grows, so J_nu(psi_k) and the
         # product weights fall towards zero and are conditioned in absolute terms
         assert np.allclose(W[row + 1, 1:], prod, rtol=1e-10, atol=1e-10 * np.abs(prod).max())
+
+
+def test_gamma0_known_answer_analytic_bispectrum(nz256):
+    """Known answer for the Gamma integrand chain (Ogata nodes, A, alpha,
+    betabar, phases, centroid rotation): with the analytic test bispectrum of
+    classed_version/bispectrum.cpp:989-996 and the Ogata settings of the
+    reference's test (h = 0.01, k up to 3.5: classed testGamma_analytical_bispectrum.cpp:94),
+    Gamma^0 equals the closed form ggg (classed gamma.cpp:567-586) in modulus
+    for every triangle, and equals -ggg for equilateral ones (the closed form's
+    sign and projection convention). Triangles from 8' up, where k <= 3.5
+    resolves the bispectrum's highest-ell components."""
+    import ctypes as C
+
+    from conftest import COSMO1
+
+    T = O.Tables(COSMO1, nz256)
+    T.set_analytic(True)
+    L = O.lib()
+    L.orc_set_ogata.argtypes = [C.c_double, C.c_int]
+    arc = 2.9088820866e-4
+    try:
+        L.orc_set_ogata(0.01, 350)
+        for tri in [(30, 30, 30), (8, 6, 3), (12, 10, 4), (50, 40, 20)]:
+            x = [t * arc for t in tri]
+            g, _ = T.gamma(0, *x, 1e-3)
+            ga = O.ggg_analytic(*x)
+            assert abs(abs(g) / abs(ga) - 1) < 1e-3, (tri, g, ga)
+            if tri[0] == tri[1] == tri[2]:
+                assert abs(g / ga + 1) < 1e-3, (tri, g, ga)
+    finally:
+        L.orc_set_ogata(0.1, 33)
+    # the default (CUDA) Ogata rule is back
+    w = O.ogata_weights()
+    assert w.shape == (4, 33)
