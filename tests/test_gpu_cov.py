@@ -157,3 +157,22 @@ def test_t1_total_symmetry(shapenoise_ctx):
     ab = shapenoise_ctx.cov_total(1, [a], [b], geometry=2, thetaMax=TMAX, area=AREA)[0]
     ba = shapenoise_ctx.cov_total(1, [b], [a], geometry=2, thetaMax=TMAX, area=AREA)[0]
     assert ab == pytest.approx(ba, rel=1e-3)
+
+
+@pytest.mark.parametrize("a,b", [((4, 4, 4), (8, 8, 8)), ((4, 4, 8), (4, 8, 8))])
+def test_white_noise_brute_force_on_gpu(nz256, a, b):
+    """The GPU T1_total/T2_total (square window, constant P) against the
+    real-space white-noise brute force of oracle/white_noise.py."""
+    import threepoint_gb300 as tp
+    from oracle import white_noise as WN
+
+    side, pix, sigma = 40 * ARC, 0.25 * ARC, 0.3
+    th123, th456 = np.array(a) * ARC, np.array(b) * ARC
+    t1, t2 = WN.t1_t2(th123, th456, side, pix, sigma)
+    ctx = tp.Context(0)
+    ctx.set_shape_noise(np.sqrt(2) * sigma, 1 / pix ** 2, True)
+    ctx.set_cosmology(tp.cosmology(**COSMO1), nz256)
+    kw = dict(geometry=tp.GEOM_SQUARE, thetaMax=side, area=side * side, precision=tp.FP64)
+    assert ctx.cov_total(1, [th123], [th456], **kw)[0] == pytest.approx(t1, rel=1e-2)
+    assert ctx.cov_total(2, [th123], [th456], **kw)[0] == pytest.approx(t2, rel=2e-3)
+    ctx.close()

@@ -160,3 +160,30 @@ def test_gamma0_known_answer_analytic_bispectrum(nz256):
     # the default (CUDA) Ogata rule is back
     w = O.ogata_weights()
     assert w.shape == (4, 33)
+
+
+WN_CASES = [((4, 4, 4), (8, 8, 8)), ((4, 4, 8), (4, 8, 8))]
+
+
+@pytest.mark.parametrize("a,b", WN_CASES)
+def test_white_noise_covariance_brute_force(nz256, a, b):
+    """Known answer for the covariance formulas (including the permutation
+    tables of T1_total and T2_total): a Gaussian white-noise field on a pixel
+    grid, whose estimator covariance is summed in real space
+    (oracle/white_noise.py, after classed testCalculateCovarianceGaussianWhiteNoise.cpp),
+    against the oracle's square-window T1_total and T2_total with the equivalent
+    constant P(ell) = sigma^2 A_pix (sigma_eps^2 = 2 sigma^2, n = 1/A_pix).
+    Tolerances: T1 is a 6-D cubature at relative tolerance 1e-2; the pixel
+    grid (0.25' for 4'-8' apertures) adds ~1e-3."""
+    from conftest import COSMO1
+    from oracle import white_noise as WN
+
+    arc = 2.9088820866e-4
+    side, pix, sigma = 40 * arc, 0.25 * arc, 0.3
+    th123, th456 = np.array(a) * arc, np.array(b) * arc
+    t1, t2 = WN.t1_t2(th123, th456, side, pix, sigma)
+    T = O.Tables(COSMO1, nz256)
+    T.set_noise(np.sqrt(2) * sigma, 1 / pix ** 2, True)
+    p = O.CovParams(1, side, side * side, 0.0)
+    assert T.cov_total(1, p, th123, th456) == pytest.approx(t1, rel=1e-2)
+    assert T.cov_total(2, p, th123, th456) == pytest.approx(t2, rel=2e-3)
