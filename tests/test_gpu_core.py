@@ -156,3 +156,23 @@ def test_region_cap_exhaustion_reports_and_recovers(nz256):
     ref = ctx.map3_batch(th, precision=tp.FP64)
     assert v2[0, 0] == pytest.approx(ref[0, 0], rel=1e-3)
     ctx.close()
+
+
+def test_bkappa_on_reference_dump_grid(gpu_ctx, oracle_tables):
+    """b_kappa on the grid of the reference's bispectrum dump program
+    (classed testApertureStatistics_bispectrum.cpp:59-65: 10 log-spaced ell on
+    [1, 1e5] x 10 ell x 10 phi on [1e-4, 2 pi]), FP64 against the oracle, and
+    the points the reference's own cut-offs set to zero (ell3 <= 1e-10)."""
+    ls = np.logspace(0, 5, 10)
+    phis = np.linspace(1e-4, 6.28308531, 10)
+    ell = np.array([(a, b, math.sqrt(max(a * a + b * b + 2 * a * b * math.cos(p), 0.0)))
+                    for a in ls for b in ls for p in phis])
+    got = gpu_ctx.bkappa(ell, precision=0)
+    ref = oracle_tables.bkappa_batch(ell)
+    nz = ref != 0
+    assert np.array_equal(got == 0, ref == 0)
+    rel = np.abs(got[nz] - ref[nz]) / np.abs(ref[nz])
+    assert np.median(rel) < 1e-13 and rel.max() < 1e-8, (np.median(rel), rel.max())
+    got32 = gpu_ctx.bkappa(ell, precision=1)
+    rel32 = np.abs(got32[nz] - ref[nz]) / np.abs(ref[nz])
+    assert np.median(rel32) < 1e-5 and rel32.max() < 1e-3, (np.median(rel32), rel32.max())
