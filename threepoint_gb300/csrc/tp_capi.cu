@@ -383,6 +383,7 @@ extern "C" int tp_ctx_destroy(tp_ctx* c) {
 
 extern "C" int tp_set_cosmologies(tp_ctx* ctx, const tp_cosmology* cosmo, int n, const double* nz, int nz_stride,
                                   const double* pk, double dk, double kmin, double kmax) {
+  TpRange nvtx_range("tp_set_cosmologies: table build");
   if (!ctx || !cosmo || n <= 0 || !nz || (nz_stride != 0 && nz_stride != NZ)) return TP_ERR_ARG;
   for (int i = 0; i < n; ++i) {
     const tp_cosmology& c = cosmo[i];
@@ -503,6 +504,7 @@ extern "C" int tp_get_tables(tp_ctx* ctx, int i, double* out) {
 // ---------------------------------------------------------------------------
 extern "C" int tp_bkappa_batch(tp_ctx* ctx, const int* cosmo_index, const double* ell, long n, int precision,
                                double* out) {
+  TpRange nvtx_range("tp_bkappa_batch");
   if (!ctx || !ell || !out || n < 0) return TP_ERR_ARG;
   if (precision != TP_FP64 && precision != TP_FP32) return TP_ERR_ARG;
   if (ctx->n_cosmo == 0) return tp_fail(ctx, TP_ERR_STATE, "no cosmology set");
@@ -545,6 +547,7 @@ extern "C" int tp_map3_jobs_device(tp_ctx* ctx, const int* job_cosmo, const doub
                                    double phi_min, double phi_max, double l_min, double l_max, double rel_tol,
                                    int precision, double* out, double* err, int64_t* neval, int64_t* nlive,
                                    int* status, const int* job_order) {
+  TpRange nvtx_range("tp_map3_jobs_device: <Map^3> launch");
   if (!ctx || !job_cosmo || !job_theta || !out || n_jobs < 0) return TP_ERR_ARG;
   if (precision != TP_FP64 && precision != TP_FP32) return TP_ERR_ARG;
   if (!(rel_tol > 0) || !(phi_max > phi_min) || !(l_min >= 0)) return TP_ERR_ARG;
@@ -591,6 +594,7 @@ extern "C" int tp_map3_jobs_device(tp_ctx* ctx, const int* job_cosmo, const doub
 extern "C" int tp_map3_batch(tp_ctx* ctx, const int* cosmo_index, int n_cosmo, const double* thetas, int n_trip,
                              double phi_min, double phi_max, double l_min, double l_max, double rel_tol,
                              int precision, double* out, double* err, int64_t* neval, int* status_out) {
+  TpRange nvtx_range("tp_map3_batch: <Map^3>");
   if (!ctx || !thetas || !out || n_cosmo <= 0 || n_trip <= 0) return TP_ERR_ARG;
   if (ctx->n_cosmo == 0) return tp_fail(ctx, TP_ERR_STATE, "no cosmology set");
   for (int t = 0; t < 3 * n_trip; ++t)

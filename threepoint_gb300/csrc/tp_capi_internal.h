@@ -1,12 +1,23 @@
 // Context object behind the opaque tp_ctx handle (host side).
 #pragma once
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include <string>
 #include <unordered_map>
 #include <vector>
 
 #include "tp_internal.cuh"
+
+// NVTX range over one entry-point call (host time: the table build, the
+// integral launches and their synchronisation), visible in Nsight tools;
+// NVTX is header-only and costs nothing without a profiler attached.
+struct TpRange {
+  explicit TpRange(const char* name) { nvtxRangePushA(name); }
+  ~TpRange() { nvtxRangePop(); }
+  TpRange(const TpRange&) = delete;
+  TpRange& operator=(const TpRange&) = delete;
+};
 
 struct tp_ctx {
   int device = 0;

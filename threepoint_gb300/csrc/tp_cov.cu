@@ -746,6 +746,7 @@ static int check_cov_args(tp_ctx* ctx, int cosmo, int term, int geom, int precis
 
 extern "C" int tp_cov_term_batch(tp_ctx* ctx, int cosmo, int term, int geometry, double theta_max, double area,
                                  const double* th6, int n, int precision, double* out, int* status_bad) {
+  TpRange nvtx_range("tp_cov_term_batch: covariance terms");
   int st = check_cov_args(ctx, cosmo, term, geometry, precision);
   if (st) return st;
   if (!th6 || !out || n < 0) return TP_ERR_ARG;
@@ -769,6 +770,7 @@ extern "C" int tp_cov_term_batch(tp_ctx* ctx, int cosmo, int term, int geometry,
 extern "C" int tp_cov_total_batch(tp_ctx* ctx, int cosmo, int term, int geometry, double theta_max, double area,
                                   const double* th123, const double* th456, int n, int precision, double* out,
                                   int* status_bad) {
+  TpRange nvtx_range("tp_cov_total_batch: covariance totals");
   int st = check_cov_args(ctx, cosmo, term, geometry, precision);
   if (st) return st;
   if (!th123 || !th456 || !out || n < 0) return TP_ERR_ARG;

@@ -409,6 +409,7 @@ extern "C" int tp_ogata_weights(double* out) {
 
 extern "C" int tp_gamma_batch(tp_ctx* ctx, int cosmo_index, const double* x, int n, int comp_mask, double rel_tol,
                               int precision, double* out, int* status_out) {
+  TpRange nvtx_range("tp_gamma_batch: Gamma");
   if (!ctx || !x || !out || n < 0 || (comp_mask & ~0xF) || comp_mask == 0) return TP_ERR_ARG;
   if (precision != TP_FP64 && precision != TP_FP32) return TP_ERR_ARG;
   if (!(rel_tol > 0)) return TP_ERR_ARG;
