@@ -353,6 +353,15 @@ __device__ __forceinline__ float2 p2sub(float2 a, float2 b) {
       : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
   return d;
 }
+__device__ __forceinline__ float2 p2add_rd(float2 a, float2 b) {  // rounded toward -inf
+  float2 d;
+  asm("{\n\t.reg .b64 ra, rb, rd;\n\t"
+      "mov.b64 ra, {%2, %3};\n\tmov.b64 rb, {%4, %5};\n\t"
+      "add.rm.f32x2 rd, ra, rb;\n\tmov.b64 {%0, %1}, rd;\n\t}"
+      : "=f"(d.x), "=f"(d.y)
+      : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+  return d;
+}
 __device__ __forceinline__ float2 p2dup(float v) { return make_float2(v, v); }
 __device__ __forceinline__ float2 p2ex2(float2 a) { return make_float2(Mth<float>::ex2(a.x), Mth<float>::ex2(a.y)); }
 __device__ __forceinline__ float2 p2rcp(float2 a) { return make_float2(Mth<float>::rcp(a.x), Mth<float>::rcp(a.y)); }
@@ -454,14 +463,22 @@ __device__ __forceinline__ float2 bispec_pair(const float2* __restrict__ c, cons
       else
         t2 = p2fma(v2(T.lg[i]), p2dup(INV), c[NF_TOFF]);
       if (K.plt) {
-        float tt[2] = {t2.x, t2.y}, r[2];
+        float2 tc = t2;
+        if constexpr (!pre) {
+          tc.x = fminf(fmaxf(tc.x, 0.f), (float)(PLT_N - 1) - 1e-3f);
+          tc.y = fminf(fmaxf(tc.y, 0.f), (float)(PLT_N - 1) - 1e-3f);
+        }
+        // floor and fraction of both lanes with packed adds: tm = 1.5 * 2^23 + floor(t)
+        const float2 big = p2dup(12582912.f);
+        const float2 tm = p2add_rd(tc, big);
+        const float2 f2 = p2sub(tc, p2sub(tm, big));
+        const float tf[2] = {f2.x, f2.y};
+        const int ixs[2] = {__float_as_int(tm.x) - 0x4B400000, __float_as_int(tm.y) - 0x4B400000};
+        float r[2];
 #pragma unroll
         for (int h = 0; h < 2; ++h) {
-          const float t = pre ? tt[h] : fminf(fmaxf(tt[h], 0.f), (float)(PLT_N - 1) - 1e-3f);
-          const float tm = __fadd_rd(t, 12582912.f);  // 1.5 * 2^23 + floor(t)
-          const int ix = __float_as_int(tm) - 0x4B400000;
-          const float f = t - (tm - 12582912.f);
-          const float4 q = reinterpret_cast<const float4*>(K.plt)[ix];
+          const float f = tf[h];
+          const float4 q = reinterpret_cast<const float4*>(K.plt)[ixs[h]];
           r[h] = M::ex2(fmaf(f, fmaf(f, fmaf(f, q.w, q.z), q.y), q.x));
         }
         pl = make_float2(r[0], r[1]);
