@@ -346,7 +346,7 @@ def run_ours(args):
                    "max_rel_err_fp32_vs_fp64": max_rel, "fp64_check_integrals": int(v64.size),
                    "zero_valued_agree": zeros_agree},
         "e2e": {"value": e2e_val, "unit": "triplets/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
-        "gpu_launches": 9 * args.steps,  # 8 table-build kernels + k_map3 per step
+        "gpu_launches": 10 * args.steps,  # 9 table-build kernels + k_map3 per step
         "roofline": {"bound": "sfu", "achieved": achieved / 1e9, "peak": sfu_peak / 1e9, "unit": "Gop/s",
                      "frac": achieved / sfu_peak, "traffic": TRAFFIC_PER_INTEGRAL * nj,
                      "traffic_unit": "bytes per launch (ncu, 880-integral capture scaled by integrals)",

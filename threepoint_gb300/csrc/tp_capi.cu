@@ -297,6 +297,7 @@ void tp_ctx::free_cosmo() {
   cudaFree(d_ck64);
   cudaFree(d_ck32);
   cudaFree(d_plt);
+  cudaFree(d_ehg);
   d_cos = nullptr;
   d_eh = nullptr;
   d_tab = nullptr;
@@ -310,6 +311,7 @@ void tp_ctx::free_cosmo() {
   d_ck64 = nullptr;
   d_ck32 = nullptr;
   d_plt = nullptr;
+  d_ehg = nullptr;
   n_cosmo = 0;
   cosmo_cap = 0;
   nz_cap = 0;
@@ -438,6 +440,7 @@ extern "C" int tp_set_cosmologies(tp_ctx* ctx, const tp_cosmology* cosmo, int n,
     if (e == cudaSuccess) e = dalloc((CosmoK<double>**)&ctx->d_ck64, cap);
     if (e == cudaSuccess) e = dalloc((CosmoK<float>**)&ctx->d_ck32, cap);
     if (e == cudaSuccess) e = dalloc(&ctx->d_plt, (size_t)cap * PLT_N);
+    if (e == cudaSuccess) e = dalloc(&ctx->d_ehg, (size_t)cap * EHG_N);
     if (e != cudaSuccess) {
       ctx->free_cosmo();
       return tp_cuda(ctx, e, "cosmology allocation");
@@ -457,7 +460,7 @@ extern "C" int tp_set_cosmologies(tp_ctx* ctx, const tp_cosmology* cosmo, int n,
   if (e == cudaSuccess)
     e = build_tables(ctx->d_cos, ctx->d_eh, ctx->d_nz, nz_stride, ctx->d_tab, ctx->d_ncoef64, ctx->d_ncoef32,
                      ctx->d_fcoef32, ctx->d_hcoef, ctx->d_hcoef32, ctx->d_wscale64, ctx->d_wscale32, (CosmoK<double>*)ctx->d_ck64,
-                     (CosmoK<float>*)ctx->d_ck32, ctx->d_plt, n, s);
+                     (CosmoK<float>*)ctx->d_ck32, ctx->d_plt, ctx->d_ehg, n, s);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);
   if (e != cudaSuccess) return tp_cuda(ctx, e, "table build");
   return TP_OK;

@@ -45,6 +45,7 @@ struct tp_ctx {
   void* d_ck64 = nullptr;
   void* d_ck32 = nullptr;
   float4* d_plt = nullptr;  // [n_cosmo][PLT_N] log2 P_lin cubic segments
+  double* d_ehg = nullptr;  // [n_cosmo][EHG_N] 2 ln T(k) of the sigma(R) integrand
 
   // shape noise of P(ell)
   double sigma_eps = 0.0, ngal = 1.0;

@@ -23,6 +23,12 @@ constexpr double LN2 = 0.69314718055994530942;
 // fit itself.
 constexpr int PLT_N = 1024;  // grid points; the table stores per interval (y0, c1, c2, c3) of the cubic
 constexpr double PLT_LO = -24.0, PLT_HI = 24.0;
+// 2 ln T(k) of the Eisenstein & Hu no-wiggle transfer function, the part of
+// the sigma(R) integrand that does not depend on R, on the grid
+// t_i = EHG_T0 + i / EHG_PER_UNIT in t = ln(k h^-1 Mpc), i < EHG_N (ln k in
+// [-16, 12]); 4-point Lagrange interpolation is within 3e-13 of the formula
+constexpr int EHG_N = 28704;
+constexpr double EHG_T0 = -16.0, EHG_PER_UNIT = 1024.0;
 
 // Per-cosmology parameter block as uploaded to the device.
 struct CosmoDev {

@@ -106,12 +106,40 @@ __device__ inline double d_window(double x, int i) {
   return (3 * (x * x - 3) * sin(x) + 9 * x * cos(x)) / x / x / x / x;
 }
 
+// Eisenstein & Hu no-wiggle transfer function L / (L + C q^2) at k [h/Mpc]
+// (bispectrum.cu:602-693, the k-dependent factor of linear_pk)
+__device__ __noinline__ double eh_transfer(const EHConst& e, double k) {
+  const double kk = k * e.h;
+  const double xs = 0.43 * kk * e.sh;
+  const double xs2 = xs * xs;
+  const double geff = e.omh2 * (e.sa + e.one_m_sa / (1.0 + xs2 * xs2));
+  const double qeff = kk / geff * e.theta2;
+  const double L = log(2.718281828 + e.c184 * qeff);
+  const double C = 14.4 + 325.0 / (1.0 + 60.5 * exp(1.11 * log(qeff)));
+  return L / (L + C * qeff * qeff);
+}
+
+// 2 ln T(e^t) from one cosmology's EHG table by 4-point Lagrange
+// interpolation; false outside the grid's interior (or for a NaN t)
+__device__ inline bool eh_table_lookup(const double* __restrict__ g, double t, double& out) {
+  const double x = (t - EHG_T0) * EHG_PER_UNIT;
+  if (!(x >= 1.0 && x < (double)(EHG_N - 2))) return false;
+  const int i = (int)x;
+  const double u = x - i, um1 = u - 1.0, um2 = u - 2.0, up1 = u + 1.0;
+  const double a = u * um1, b = up1 * um2;
+  // weights -a(u-2)/6, b(u-1)/2, -b u/2, a(u+1)/6 on g[i-1], g[i], g[i+1], g[i+2]
+  out = a * (up1 * g[i + 2] - um2 * g[i - 1]) * (1.0 / 6.0) + b * (um1 * g[i] - u * g[i + 1]) * 0.5;
+  return true;
+}
+
 // Integrand in ln k of sigmam (bispectrum.cu:823-832): k^3 P(k) W(kr)^2 for
 // j < 3, k^3 P(k) W(kr) for j = 3, at k = exp(t). For the Gaussian windows
-// (j = 1..3) the powers k^3, (kh)^ns and exp(-(kr)^2) are folded into one exp;
-// the values agree with the literal form to rounding.
+// (j = 1..3) the powers k^3, (kh)^ns, exp(-(kr)^2) and the squared transfer
+// function are folded into one exp; the values agree with the literal form
+// to rounding. ehg (or null) is the cosmology's EHG table of 2 ln T, used
+// inside its grid: the integrand then agrees with the formula to 3e-13.
 __device__ inline double sigma_integrand(const CosmoDev& c, const EHConst& e, const double* pk, double k, double t,
-                                         double r, int j, double lnh, double lnkmin) {
+                                         double r, int j, double lnh, double lnkmin, const double* ehg) {
   if (j == 0) {
     double w = d_window(k * r, 0);
     return k * k * k * d_linear_pk(c, e, pk, k) * w * w;
@@ -133,15 +161,13 @@ __device__ inline double sigma_integrand(const CosmoDev& c, const EHConst& e, co
     v = exp(3.0 * t - x2) * p;
   } else {
     // Eisenstein & Hu no-wiggle shape (bispectrum.cu:602-693) times k^3 W^2
-    const double kk = k * e.h;
-    const double xs = 0.43 * kk * e.sh;
-    const double xs2 = xs * xs;
-    const double geff = e.omh2 * (e.sa + e.one_m_sa / (1.0 + xs2 * xs2));
-    const double qeff = kk / geff * e.theta2;
-    const double L = log(2.718281828 + e.c184 * qeff);
-    const double C = 14.4 + 325.0 / (1.0 + 60.5 * exp(1.11 * log(qeff)));
-    const double rr = L / (L + C * qeff * qeff);
-    v = e.ehc * exp((3.0 + e.ns) * t + e.ns * lnh - x2) * rr * rr;
+    double g2;
+    if (ehg && eh_table_lookup(ehg, t, g2)) {
+      v = e.ehc * exp((3.0 + e.ns) * t + e.ns * lnh - x2 + g2);
+    } else {
+      const double rr = eh_transfer(e, k);
+      v = e.ehc * exp((3.0 + e.ns) * t + e.ns * lnh - x2) * rr * rr;
+    }
   }
   if (j == 1) return v;
   if (j == 2) return v * x2;
@@ -154,12 +180,14 @@ __device__ inline double sigma_integrand(const CosmoDev& c, const EHConst& e, co
 // doubling evaluates only the new odd points and adds them to the previous
 // level's sum: the even points of level n are bitwise the points of level n/2
 // (hh is halved exactly), so this is the reference's sum in another order.
-__device__ double warp_sigmam(const CosmoDev& c, const EHConst& e, const double* pk, double r, int j) {
+__device__ double warp_sigmam(const CosmoDev& c, const EHConst& e, const double* pk, double r, int j,
+                              const double* ehg = nullptr) {
   if (c.sigma8 < 1e-8) return 0;
   const int lane = threadIdx.x & 31;
   const double lnh = log(e.h), lnkmin = c.pk_given ? log(c.kmin) : 0.0;
   double k1 = 2. * PI / r, k2 = 2. * PI / r;
   double xx = 0, xxpp = -1.0;
+  const bool run_k = ehg && j > 0 && !c.pk_given;
   // iteration caps: at most 2^22 trapezoid points per pass; a non-finite sum
   // (only for invalid cosmologies) ends the iteration
   for (int outer = 0; outer < 40; ++outer) {
@@ -168,7 +196,8 @@ __device__ double warp_sigmam(const CosmoDev& c, const EHConst& e, const double*
     double a = log(k1), b = log(k2);
     double xxp = -1.0;
     int n = 2;
-    double ends = 0.5 * (sigma_integrand(c, e, pk, k1, a, r, j, lnh, lnkmin) + sigma_integrand(c, e, pk, k2, b, r, j, lnh, lnkmin));
+    double ends = 0.5 * (sigma_integrand(c, e, pk, k1, a, r, j, lnh, lnkmin, ehg) +
+                         sigma_integrand(c, e, pk, k2, b, r, j, lnh, lnkmin, ehg));
     double sum = 0;
     for (int inner = 0; inner < 21; ++inner) {
       n = n * 2;
@@ -177,12 +206,24 @@ __device__ double warp_sigmam(const CosmoDev& c, const EHConst& e, const double*
       if (n == 4) {  // first level: all three interior points
         for (int i = 1 + lane; i < 4; i += 32) {
           double t = a + hh * i;
-          part += sigma_integrand(c, e, pk, exp(t), t, r, j, lnh, lnkmin);
+          part += sigma_integrand(c, e, pk, exp(t), t, r, j, lnh, lnkmin, ehg);
+        }
+      } else if (run_k) {
+        // k = e^t by a running product along the lane's points (a relative
+        // error below 1e-14 in k, which enters only through exp(-(kr)^2))
+        if (lane < n / 2) {
+          const double step = exp(64.0 * hh);
+          double k = exp(a + hh * (2 * lane + 1));
+          for (int m = lane; m < n / 2; m += 32) {
+            const double t = a + hh * (2 * m + 1);
+            part += sigma_integrand(c, e, pk, k, t, r, j, lnh, lnkmin, ehg);
+            k *= step;
+          }
         }
       } else {
         for (int m = lane; m < n / 2; m += 32) {
           double t = a + hh * (2 * m + 1);
-          part += sigma_integrand(c, e, pk, exp(t), t, r, j, lnh, lnkmin);
+          part += sigma_integrand(c, e, pk, exp(t), t, r, j, lnh, lnkmin, ehg);
         }
       }
       for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
@@ -296,9 +337,19 @@ __global__ void k_growth(const CosmoDev* cos, TablesDev* tab, int n) {
   tab[ci].D1[i] = d_lgr(c, (i + 0.5) * (c.zmax / NZ)) / tab[ci].lgr0;
 }
 
+// 2 ln T(k) of the Eisenstein & Hu fit on the EHG grid, one thread per
+// (cosmology, grid point); shape constants only, so it runs before k_norm
+__global__ void k_eh_table(const CosmoDev* cos, const EHConst* eh, double* ehg, int n) {
+  const long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int ci = (int)(idx / EHG_N), i = (int)(idx % EHG_N);
+  if (ci >= n || cos[ci].pk_given) return;
+  const double t = EHG_T0 + i / EHG_PER_UNIT;
+  ehg[(size_t)ci * EHG_N + i] = 2.0 * log(eh_transfer(eh[ci], exp(t)));
+}
+
 // r_sigma by bisection on D1 sigma(1/k) = 1, then n_eff and ncur
 // (bispectrum.cu:202-212, 870-903); one warp per (cosmology, bin)
-__global__ void k_rsigma(const CosmoDev* cos, const EHConst* eh, TablesDev* tab, int n) {
+__global__ void k_rsigma(const CosmoDev* cos, const EHConst* eh, TablesDev* tab, const double* ehg_all, int n) {
   int wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   int ci = wid / NZ, bin = wid % NZ;
   if (ci >= n) return;
@@ -306,19 +357,20 @@ __global__ void k_rsigma(const CosmoDev* cos, const EHConst* eh, TablesDev* tab,
   const EHConst e = eh[ci];
   TablesDev& t = tab[ci];
   const double* pk = t.pk;
+  const double* ehg = ehg_all + (size_t)ci * EHG_N;
   double D1 = t.D1[bin];
   double rs = 0;
   if (c.sigma8 >= 1e-8) {
     double k, k1 = 1., k2 = 1.;
     bool bad = !isfinite(D1);
     for (int it = 0; it < 100 && !bad; ++it) {
-      double s = D1 * warp_sigmam(c, e, pk, 1. / k1, 1);
+      double s = D1 * warp_sigmam(c, e, pk, 1. / k1, 1, ehg);
       if (!isfinite(s)) bad = true;
       if (s < 1. || bad) break;
       k1 *= 0.5;
     }
     for (int it = 0; it < 100 && !bad; ++it) {
-      double s = D1 * warp_sigmam(c, e, pk, 1. / k2, 1);
+      double s = D1 * warp_sigmam(c, e, pk, 1. / k2, 1, ehg);
       if (!isfinite(s)) bad = true;
       if (s > 1. || bad) break;
       k2 *= 2.;
@@ -326,7 +378,7 @@ __global__ void k_rsigma(const CosmoDev* cos, const EHConst* eh, TablesDev* tab,
     k = 0.5 * (k1 + k2);
     for (int it = 0; it < 200 && !bad; ++it) {
       k = 0.5 * (k1 + k2);
-      double s = D1 * warp_sigmam(c, e, pk, 1. / k, 1);
+      double s = D1 * warp_sigmam(c, e, pk, 1. / k, 1, ehg);
       if (!isfinite(s)) {
         bad = true;
         break;
@@ -339,8 +391,8 @@ __global__ void k_rsigma(const CosmoDev* cos, const EHConst* eh, TablesDev* tab,
     }
     rs = bad ? NAN : 1. / k;
   }
-  double s2 = isfinite(rs) ? warp_sigmam(c, e, pk, rs, 2) : NAN;
-  double s3 = isfinite(rs) ? warp_sigmam(c, e, pk, rs, 3) : NAN;
+  double s2 = isfinite(rs) ? warp_sigmam(c, e, pk, rs, 2, ehg) : NAN;
+  double s3 = isfinite(rs) ? warp_sigmam(c, e, pk, rs, 3, ehg) : NAN;
   if ((threadIdx.x & 31) == 0) {
     double d1 = -2. * (D1 * s2) * (D1 * s2);
     t.r_sigma[bin] = rs;
@@ -592,8 +644,8 @@ void upload_gauss_nodes() {
 cudaError_t build_tables(const CosmoDev* d_cos, EHConst* d_eh, const double* d_nz, int nz_stride, TablesDev* d_tab,
                          double* d_ncoef, float* d_ncoef_f, float* d_fcoef_f, double* d_hcoef, float* d_hcoef_f,
                          double* d_wscale64,
-                         double* d_wscale32, CosmoK<double>* d_ck64, CosmoK<float>* d_ck32, float4* d_plt, int n,
-                         cudaStream_t s) {
+                         double* d_wscale32, CosmoK<double>* d_ck64, CosmoK<float>* d_ck32, float4* d_plt,
+                         double* d_ehg, int n, cudaStream_t s) {
   // every launch is made of one-warp blocks (see above). An SM runs blocks of
   // different kernels together only in one shared-memory/L1 configuration:
   // these kernels ask for the one k_map3 runs in (maximum shared memory).
@@ -601,18 +653,19 @@ cudaError_t build_tables(const CosmoDev* d_cos, EHConst* d_eh, const double* d_n
   int dev = 0;
   cudaGetDevice(&dev);
   if (carveout_set != dev) {
-    const void* ks[] = {(const void*)k_norm, (const void*)k_fk, (const void*)k_g, (const void*)k_growth,
+    const void* ks[] = {(const void*)k_eh_table, (const void*)k_norm, (const void*)k_fk, (const void*)k_g, (const void*)k_growth,
                         (const void*)k_rsigma, (const void*)k_node_coefs, (const void*)k_finish,
                         (const void*)k_plin_table};
     for (const void* k : ks)
       cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
     carveout_set = dev;
   }
+  k_eh_table<<<(unsigned)((long)n * EHG_N / 32), 32, 0, s>>>(d_cos, d_eh, d_ehg, n);
   k_norm<<<n, 32, 0, s>>>(d_cos, d_eh, d_tab, n);
   k_fk<<<n * (NZ / 32), 32, 0, s>>>(d_cos, d_tab, n);
   k_g<<<n * (NZ / 32), 32, 0, s>>>(d_cos, d_nz, nz_stride, d_tab, n);
   k_growth<<<n * (NZ / 32), 32, 0, s>>>(d_cos, d_tab, n);
-  k_rsigma<<<(unsigned)((long)n * NZ), 32, 0, s>>>(d_cos, d_eh, d_tab, n);
+  k_rsigma<<<(unsigned)((long)n * NZ), 32, 0, s>>>(d_cos, d_eh, d_tab, d_ehg, n);
   k_node_coefs<<<n * (NNODE / 32), 32, 0, s>>>(d_cos, d_tab, d_ncoef, d_ncoef_f, d_fcoef_f, d_hcoef, d_hcoef_f, n);
   k_finish<<<n, 32, 0, s>>>(d_cos, d_eh, d_tab, d_ncoef, d_ncoef_f, d_fcoef_f, d_wscale64, d_wscale32, d_ck64, d_ck32,
                             n);

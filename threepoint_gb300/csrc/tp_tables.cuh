@@ -15,7 +15,7 @@ void upload_gauss_nodes();
 cudaError_t build_tables(const CosmoDev* d_cos, EHConst* d_eh, const double* d_nz, int nz_stride, TablesDev* d_tab,
                          double* d_ncoef, float* d_ncoef_f, float* d_fcoef_f, double* d_hcoef, float* d_hcoef_f,
                          double* d_wscale64,
-                         double* d_wscale32, CosmoK<double>* d_ck64, CosmoK<float>* d_ck32, float4* d_plt, int n,
-                         cudaStream_t s);
+                         double* d_wscale32, CosmoK<double>* d_ck64, CosmoK<float>* d_ck32, float4* d_plt,
+                         double* d_ehg, int n, cudaStream_t s);
 
 }  // namespace tp
