@@ -278,14 +278,21 @@ __device__ double d_lgr(const CosmoDev& c, double z) {
 // kernels
 // ---------------------------------------------------------------------------
 
-// The table kernels run as one-warp blocks: a block needs at most 128 x 32
-// registers and a few KB of shared memory, so it fits beside three resident
-// k_map3 CTAs and the next batch's tables build on the FP64 pipe while the
-// current batch integrates.
+// The table kernels run as one-warp blocks of at most TP_TABLES_MAXNREG
+// registers a thread. An SM's registers are split between its four
+// sub-partitions (16384 each) and a warp takes its registers from one of
+// them: three resident k_map3<float> CTAs (6 warps of 80 registers per
+// sub-partition) leave 1024 registers in each, room for one 32-register
+// warp. With the cap the next batch's tables build on the FP64 pipe while
+// the current batch integrates, at the cost of spills to L1.
+#ifndef TP_TABLES_MAXNREG
+#define TP_TABLES_MAXNREG 32
+#endif
+#define TP_TABLE_KERNEL __global__ void __maxnreg__(TP_TABLES_MAXNREG)
 
 // norm = sigma8 / sigma(8 Mpc/h, top hat) and the growth integral at z = 0;
 // one warp per cosmology
-__global__ void k_norm(const CosmoDev* cos, EHConst* eh, TablesDev* tab, int n) {
+TP_TABLE_KERNEL k_norm(const CosmoDev* cos, EHConst* eh, TablesDev* tab, int n) {
   int ci = blockIdx.x;
   if (ci >= n) return;
   CosmoDev c = cos[ci];
@@ -302,7 +309,7 @@ __global__ void k_norm(const CosmoDev* cos, EHConst* eh, TablesDev* tab, int n) 
 
 // f_K on bin centres (bispectrum.cu:158-166); block b of a cosmology takes
 // bins 32 b .. 32 b + 31
-__global__ void k_fk(const CosmoDev* cos, TablesDev* tab, int n) {
+TP_TABLE_KERNEL k_fk(const CosmoDev* cos, TablesDev* tab, int n) {
   const int ci = blockIdx.x / (NZ / 32), i = (blockIdx.x % (NZ / 32)) * 32 + threadIdx.x;
   if (ci >= n) return;
   const CosmoDev c = cos[ci];
@@ -314,7 +321,7 @@ __global__ void k_fk(const CosmoDev* cos, TablesDev* tab, int n) {
 }
 
 // lensing efficiency g by the trapezoid sum over n(z) (bispectrum.cu:168-190)
-__global__ void k_g(const CosmoDev* cos, const double* nz, int nz_stride, TablesDev* tab, int n) {
+TP_TABLE_KERNEL k_g(const CosmoDev* cos, const double* nz, int nz_stride, TablesDev* tab, int n) {
   const int ci = blockIdx.x / (NZ / 32), i = (blockIdx.x % (NZ / 32)) * 32 + threadIdx.x;
   if (ci >= n) return;
   const double dz = cos[ci].zmax / NZ;
@@ -330,7 +337,7 @@ __global__ void k_g(const CosmoDev* cos, const double* nz, int nz_stride, Tables
 }
 
 // linear growth D1 = lgr(z)/lgr(0) on bin centres (bispectrum.cu:207)
-__global__ void k_growth(const CosmoDev* cos, TablesDev* tab, int n) {
+TP_TABLE_KERNEL k_growth(const CosmoDev* cos, TablesDev* tab, int n) {
   const int ci = blockIdx.x / (NZ / 32), i = (blockIdx.x % (NZ / 32)) * 32 + threadIdx.x;
   if (ci >= n) return;
   const CosmoDev c = cos[ci];
@@ -339,7 +346,7 @@ __global__ void k_growth(const CosmoDev* cos, TablesDev* tab, int n) {
 
 // 2 ln T(k) of the Eisenstein & Hu fit on the EHG grid, one thread per
 // (cosmology, grid point); shape constants only, so it runs before k_norm
-__global__ void k_eh_table(const CosmoDev* cos, const EHConst* eh, double* ehg, int n) {
+TP_TABLE_KERNEL k_eh_table(const CosmoDev* cos, const EHConst* eh, double* ehg, int n) {
   const long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
   const int ci = (int)(idx / EHG_N), i = (int)(idx % EHG_N);
   if (ci >= n || cos[ci].pk_given) return;
@@ -349,7 +356,7 @@ __global__ void k_eh_table(const CosmoDev* cos, const EHConst* eh, double* ehg, 
 
 // r_sigma by bisection on D1 sigma(1/k) = 1, then n_eff and ncur
 // (bispectrum.cu:202-212, 870-903); one warp per (cosmology, bin)
-__global__ void k_rsigma(const CosmoDev* cos, const EHConst* eh, TablesDev* tab, const double* ehg_all, int n) {
+TP_TABLE_KERNEL k_rsigma(const CosmoDev* cos, const EHConst* eh, TablesDev* tab, const double* ehg_all, int n) {
   int wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   int ci = wid / NZ, bin = wid % NZ;
   if (ci >= n) return;
@@ -426,7 +433,7 @@ __device__ inline double interp_mid(const double* arr, double zfrac_bins) {
 // Per-node coefficients of b_kappa's LOS integral (z-only parts of
 // integrand_bkappa + bispec, bispectrum.cu:221-333) and of P_kappa's
 // (limber_integrand_power_spectrum + P_k_nonlinear, bispectrum.cu:531-600,951-991).
-__global__ void k_node_coefs(const CosmoDev* cos, const TablesDev* tab, double* ncoef, float* ncoef_f, float* fcoef_f,
+TP_TABLE_KERNEL k_node_coefs(const CosmoDev* cos, const TablesDev* tab, double* ncoef, float* ncoef_f, float* fcoef_f,
                              double* hcoef, float* hcoef_f, int n) {
   // one warp per 32 nodes of a cosmology
   int ci = blockIdx.x / (NNODE / 32);
@@ -565,7 +572,7 @@ __global__ void k_node_coefs(const CosmoDev* cos, const TablesDev* tab, double* 
 // Normalise the LOS weights of the FP32 node table by their maximum (kept in
 // wscale) so that FP32 products stay far from the float range limits, and
 // build the integrand constant blocks.
-__global__ void k_finish(const CosmoDev* cos, const EHConst* eh, const TablesDev* tab, double* ncoef, float* ncoef_f,
+TP_TABLE_KERNEL k_finish(const CosmoDev* cos, const EHConst* eh, const TablesDev* tab, double* ncoef, float* ncoef_f,
                          float* fcoef_f, double* wscale64, double* wscale32, CosmoK<double>* ck64, CosmoK<float>* ck32,
                          int n) {
   int ci = blockIdx.x;
@@ -603,7 +610,7 @@ __global__ void k_finish(const CosmoDev* cos, const EHConst* eh, const TablesDev
 
 // log2 P_lin on the FP32 interpolation grid (log2(k h) uniform on [PLT_LO, PLT_HI])
 // and its Catmull-Rom cubic per interval i: y(i + f) = y0 + f (c1 + f (c2 + f c3))
-__global__ void k_plin_table(const CosmoDev* cos, const EHConst* eh, float4* plt, CosmoK<float>* ck32, int n) {
+TP_TABLE_KERNEL k_plin_table(const CosmoDev* cos, const EHConst* eh, float4* plt, CosmoK<float>* ck32, int n) {
   // block b of a cosmology builds intervals [b * PLT_SLICE, (b + 1) * PLT_SLICE)
   constexpr int PLT_SLICE = 128;
   const int ci = blockIdx.x / (PLT_N / PLT_SLICE), a = (blockIdx.x % (PLT_N / PLT_SLICE)) * PLT_SLICE;
