@@ -94,6 +94,22 @@ def test_map3_fp32_against_fp64(gpu_ctx):
     assert rel.max() < 1e-3, rel
 
 
+def test_map3_fp32_against_fp64_wide_radii(gpu_ctx):
+    """FP32 against FP64 over radii 0.5' to 100' (ell up to 7e4 at the
+    smallest radius): the FP32 node evaluation (packed pairs, merged
+    reciprocals with their out-of-range fallback) stays within 1e-3."""
+    radii = (0.5, 2.0, 8.0, 32.0, 100.0)
+    trip = [(a, b, c) for i, a in enumerate(radii) for j, b in enumerate(radii[i:], i)
+            for c in radii[j:]][::2]
+    th = [[a * ARC, b * ARC, c * ARC] for a, b, c in trip]
+    v64 = gpu_ctx.map3_batch(th, precision=0)
+    v32 = gpu_ctx.map3_batch(th, precision=1)
+    assert np.array_equal(v32 == 0, v64 == 0)
+    nz = v64 != 0
+    rel = np.abs(v32[nz] - v64[nz]) / np.abs(v64[nz])
+    assert rel.max() < 1e-3, (rel.max(), np.array(trip)[np.argmax(np.abs(v32 - v64)[0])])
+
+
 def test_map3_zero_for_disjoint_filters(gpu_ctx, oracle_tables):
     # (1', 1.47', 32'): all 33 points of the first rule have a zero filter
     # product in FP64, so the reference's cubature stops at 0 after one region

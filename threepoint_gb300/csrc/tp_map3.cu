@@ -201,14 +201,15 @@ struct Map3Policy {
       TriF2 T2;  // pairs held in registers across the node loop
       trif2_from(r.tri, T2, K.lgp_lo, K.lgp_hi);
 #endif
-      // A NaN node (bispectrum.cu:327-331 sets it to 0) or an infinite one
+      // Nodes with merged reciprocals. A NaN node (bispectrum.cu:327-331 sets
+      // it to 0), an infinite one or a merged product out of the float range
       // makes the Kahan sum non-finite: then, rarely, the group is summed
-      // again with the per-node zeroing, which gives the same result as
-      // zeroing on every node.
+      // again with separate reciprocals and the per-node zeroing, which gives
+      // the same result as zeroing on every node.
       float2 s = make_float2(0.f, 0.f), cmp = make_float2(0.f, 0.f);
       TP_UNROLL(TP_MAP3_UNROLL)
       for (int p = j0 / 2; p < (j0 + NPG) / 2; ++p) {
-        const float2 v = bispec_pair_node(s_nc, p, T2, K);
+        const float2 v = bispec_pair_node<std::remove_cv_t<std::remove_reference_t<decltype(T2)>>, true>(s_nc, p, T2, K);
         const float2 y = p2sub(v, cmp);
         const float2 t = p2add(s, y);
         cmp = p2sub(p2sub(t, s), y);
