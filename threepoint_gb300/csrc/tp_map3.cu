@@ -227,7 +227,7 @@ struct Map3Policy {
           s = t;
         }
       }
-      pv[0] = (double)s.x + (double)s.y;
+      pv[0] = (double)(s.x + s.y);  // lanes added in FP32: one conversion, no FP64 add per item
     } else {
       KSum<R> acc;
       TP_UNROLL(TP_MAP3_UNROLL)
