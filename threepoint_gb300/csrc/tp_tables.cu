@@ -289,6 +289,9 @@ __device__ double d_lgr(const CosmoDev& c, double z) {
 #define TP_TABLES_MAXNREG 32
 #endif
 #define TP_TABLE_KERNEL __global__ void __maxnreg__(TP_TABLES_MAXNREG)
+#ifndef TP_RSIGMA_SMEM
+#define TP_RSIGMA_SMEM 8192
+#endif
 
 // norm = sigma8 / sigma(8 Mpc/h, top hat) and the growth integral at z = 0;
 // one warp per cosmology
@@ -672,7 +675,12 @@ cudaError_t build_tables(const CosmoDev* d_cos, EHConst* d_eh, const double* d_n
   k_fk<<<n * (NZ / 32), 32, 0, s>>>(d_cos, d_tab, n);
   k_g<<<n * (NZ / 32), 32, 0, s>>>(d_cos, d_nz, nz_stride, d_tab, n);
   k_growth<<<n * (NZ / 32), 32, 0, s>>>(d_cos, d_tab, n);
-  k_rsigma<<<(unsigned)((long)n * NZ), 32, 0, s>>>(d_cos, d_eh, d_tab, d_ehg, n);
+  // k_rsigma (FP64-pipe bound) also takes TP_RSIGMA_SMEM bytes of shared
+  // memory it does not use: beside three k_map3 CTAs, which leave ~15 KB of an
+  // SM's shared memory, that admits one of its warps per SM instead of four,
+  // so it contends less with k_map3's own FP64 instructions; alone it still
+  // fills the SM
+  k_rsigma<<<(unsigned)((long)n * NZ), 32, TP_RSIGMA_SMEM, s>>>(d_cos, d_eh, d_tab, d_ehg, n);
   k_node_coefs<<<n * (NNODE / 32), 32, 0, s>>>(d_cos, d_tab, d_ncoef, d_ncoef_f, d_fcoef_f, d_hcoef, d_hcoef_f, n);
   k_finish<<<n, 32, 0, s>>>(d_cos, d_eh, d_tab, d_ncoef, d_ncoef_f, d_fcoef_f, d_wscale64, d_wscale32, d_ck64, d_ck32,
                             n);
