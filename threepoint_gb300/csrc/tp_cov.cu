@@ -339,18 +339,32 @@ struct BkProd {
     const int i = g >> 3, ch = g & 7;
     const int j0 = ch * 12;
     if constexpr (sizeof(R) == 4) {
-      // two nodes per step in packed FP32 pairs; Kahan sum per lane
+      // two nodes per step in packed FP32 pairs with merged reciprocals;
+      // Kahan sum per lane. A non-finite sum (a NaN node, which
+      // bispectrum.cu:327-331 sets to 0, or a merged product out of the float
+      // range) sends the group to the separate-reciprocal form with per-node
+      // zeroing.
       float2 sm = make_float2(0.f, 0.f), cmp = make_float2(0.f, 0.f);
       for (int p = j0 / 2; p < (j0 + 12) / 2; ++p) {
-        float2 v = bispec_pair_node(s_nc, p, r.t[i], ck);
-        if (v.x != v.x) v.x = 0.f;
-        if (v.y != v.y) v.y = 0.f;
+        const float2 v = bispec_pair_node<std::remove_cv_t<std::remove_reference_t<decltype(r.t[i])>>, true>(s_nc, p, r.t[i], ck);
         const float2 y = p2sub(v, cmp);
         const float2 t = p2add(sm, y);
         cmp = p2sub(p2sub(t, sm), y);
         sm = t;
       }
-      pv[0] = (double)sm.x + (double)sm.y;
+      if (!isfinite(sm.x + sm.y)) {
+        sm = make_float2(0.f, 0.f), cmp = make_float2(0.f, 0.f);
+        for (int p = j0 / 2; p < (j0 + 12) / 2; ++p) {
+          float2 v = bispec_pair_node(s_nc, p, r.t[i], ck);
+          if (v.x != v.x) v.x = 0.f;
+          if (v.y != v.y) v.y = 0.f;
+          const float2 y = p2sub(v, cmp);
+          const float2 t = p2add(sm, y);
+          cmp = p2sub(p2sub(t, sm), y);
+          sm = t;
+        }
+      }
+      pv[0] = (double)(sm.x + sm.y);
     } else {
       KSum<R> acc;
 #pragma unroll 2
