@@ -358,52 +358,97 @@ TP_TABLE_KERNEL k_eh_table(const CosmoDev* cos, const EHConst* eh, double* ehg, 
 }
 
 // r_sigma by bisection on D1 sigma(1/k) = 1, then n_eff and ncur
-// (bispectrum.cu:202-212, 870-903); one warp per (cosmology, bin)
+// (bispectrum.cu:202-212, 870-903). One warp takes RS_BINS adjacent redshift
+// bins of a cosmology; lane b < RS_BINS holds bin b's bisection as a state
+// machine that advances one iteration of the one-bin loops per round. sigma(R)
+// does not depend on the bin, and while adjacent bins' brackets coincide they
+// ask for sigma at bitwise the same k: each round the warp evaluates every
+// distinct k once (all 32 lanes in the trapezoid sums) and hands the value to
+// the bins that asked for it. Every bin sees the same sequence of values and
+// makes the same decisions as alone, with ~40% fewer sigma(R) integrals.
+constexpr int RS_BINS = 8;
+static_assert(NZ % RS_BINS == 0 && RS_BINS <= 32, "bins per warp");
+
 TP_TABLE_KERNEL k_rsigma(const CosmoDev* cos, const EHConst* eh, TablesDev* tab, const double* ehg_all, int n) {
-  int wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  int ci = wid / NZ, bin = wid % NZ;
+  const unsigned FULL = 0xffffffffu;
+  const int ci = blockIdx.x / (NZ / RS_BINS), b0 = (blockIdx.x % (NZ / RS_BINS)) * RS_BINS;
   if (ci >= n) return;
+  const int lane = threadIdx.x & 31;
   const CosmoDev c = cos[ci];
   const EHConst e = eh[ci];
   TablesDev& t = tab[ci];
   const double* pk = t.pk;
   const double* ehg = ehg_all + (size_t)ci * EHG_N;
-  double D1 = t.D1[bin];
-  double rs = 0;
-  if (c.sigma8 >= 1e-8) {
-    double k, k1 = 1., k2 = 1.;
-    bool bad = !isfinite(D1);
-    for (int it = 0; it < 100 && !bad; ++it) {
-      double s = D1 * warp_sigmam(c, e, pk, 1. / k1, 1, ehg);
-      if (!isfinite(s)) bad = true;
-      if (s < 1. || bad) break;
-      k1 *= 0.5;
+  const bool mine = lane < RS_BINS;
+  const int bin = b0 + (mine ? lane : 0);
+  const double D1 = t.D1[bin];
+  // phase 0: k1 halving (<= 100 steps), 1: k2 doubling (<= 100), 2: bisection
+  // (<= 200), 3: done; the loop limits and exits of the one-bin version
+  enum { HALVE = 0, DOUBLE = 1, BISECT = 2, DONE = 3 };
+  double k1 = 1., k2 = 1., k = 0.;
+  int phase = DONE, it = 0;
+  bool bad = false;
+  if (mine && c.sigma8 >= 1e-8) {
+    bad = !isfinite(D1);
+    phase = bad ? DONE : HALVE;
+  }
+  for (int round = 0; round < 400; ++round) {
+    const double kq = phase == HALVE ? k1 : phase == DOUBLE ? k2 : 0.5 * (k1 + k2);
+    unsigned pending = __ballot_sync(FULL, phase != DONE);
+    if (!pending) break;
+    double sg = 0;
+    while (pending) {
+      const double kv = __shfl_sync(FULL, kq, __ffs(pending) - 1);
+      const double v = warp_sigmam(c, e, pk, 1. / kv, 1, ehg);
+      const bool match = ((pending >> lane) & 1u) && kq == kv;
+      if (match) sg = v;
+      pending &= ~__ballot_sync(FULL, match);
     }
-    for (int it = 0; it < 100 && !bad; ++it) {
-      double s = D1 * warp_sigmam(c, e, pk, 1. / k2, 1, ehg);
+    if (phase == DONE) continue;
+    const double s = D1 * sg;
+    if (phase == HALVE) {
       if (!isfinite(s)) bad = true;
-      if (s > 1. || bad) break;
-      k2 *= 2.;
-    }
-    k = 0.5 * (k1 + k2);
-    for (int it = 0; it < 200 && !bad; ++it) {
-      k = 0.5 * (k1 + k2);
-      double s = D1 * warp_sigmam(c, e, pk, 1. / k, 1, ehg);
+      if (s < 1. || bad) {
+        phase = bad ? DONE : DOUBLE;
+        it = 0;
+      } else {
+        k1 *= 0.5;
+        if (++it == 100) phase = DOUBLE, it = 0;
+      }
+    } else if (phase == DOUBLE) {
+      if (!isfinite(s)) bad = true;
+      if (s > 1. || bad) {
+        phase = bad ? DONE : BISECT;
+        it = 0;
+      } else {
+        k2 *= 2.;
+        if (++it == 100) phase = BISECT, it = 0;
+      }
+    } else {
+      k = kq;
       if (!isfinite(s)) {
         bad = true;
-        break;
+        phase = DONE;
+      } else {
+        if (s < 1.)
+          k1 = k;
+        else if (s > 1.)
+          k2 = k;
+        if (s == 1. || fabs(k2 / k1 - 1.) < EPS * 0.1 || ++it == 200) phase = DONE;
       }
-      if (s < 1.)
-        k1 = k;
-      else if (s > 1.)
-        k2 = k;
-      if (s == 1. || fabs(k2 / k1 - 1.) < EPS * 0.1) break;
     }
-    rs = bad ? NAN : 1. / k;
   }
-  double s2 = isfinite(rs) ? warp_sigmam(c, e, pk, rs, 2, ehg) : NAN;
-  double s3 = isfinite(rs) ? warp_sigmam(c, e, pk, rs, 3, ehg) : NAN;
-  if ((threadIdx.x & 31) == 0) {
+  const double rs = (c.sigma8 >= 1e-8) ? (bad ? NAN : 1. / k) : 0.0;
+  // n_eff and ncur need sigma at each bin's own radius: one bin after another
+  double s2 = NAN, s3 = NAN;
+  for (int b = 0; b < RS_BINS; ++b) {
+    const double rb = __shfl_sync(FULL, rs, b);
+    if (!isfinite(rb)) continue;
+    const double v2 = warp_sigmam(c, e, pk, rb, 2, ehg);
+    const double v3 = warp_sigmam(c, e, pk, rb, 3, ehg);
+    if (lane == b) s2 = v2, s3 = v3;
+  }
+  if (mine) {
     double d1 = -2. * (D1 * s2) * (D1 * s2);
     t.r_sigma[bin] = rs;
     t.n_eff[bin] = -3. + 2. * (D1 * s2) * (D1 * s2);
@@ -680,7 +725,7 @@ cudaError_t build_tables(const CosmoDev* d_cos, EHConst* d_eh, const double* d_n
   // SM's shared memory, that admits one of its warps per SM instead of four,
   // so it contends less with k_map3's own FP64 instructions; alone it still
   // fills the SM
-  k_rsigma<<<(unsigned)((long)n * NZ), 32, TP_RSIGMA_SMEM, s>>>(d_cos, d_eh, d_tab, d_ehg, n);
+  k_rsigma<<<(unsigned)((long)n * (NZ / RS_BINS)), 32, TP_RSIGMA_SMEM, s>>>(d_cos, d_eh, d_tab, d_ehg, n);
   k_node_coefs<<<n * (NNODE / 32), 32, 0, s>>>(d_cos, d_tab, d_ncoef, d_ncoef_f, d_fcoef_f, d_hcoef, d_hcoef_f, n);
   k_finish<<<n, 32, 0, s>>>(d_cos, d_eh, d_tab, d_ncoef, d_ncoef_f, d_fcoef_f, d_wscale64, d_wscale32, d_ck64, d_ck32,
                             n);
