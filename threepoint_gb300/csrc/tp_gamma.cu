@@ -342,14 +342,7 @@ __global__ void __launch_bounds__(NT, sizeof(R) == 4 ? TP_GAMMA_MINB : 1) k_gamm
 
 template <typename R>
 static size_t gamma_smem_bytes() {
-  typedef GammaPolicy<R> P;
-  constexpr int NP = GMRule<3>::NP;
-  size_t b = (P::PSMEM + 15) & ~size_t(15);
-  b += ((size_t)P::CH * NP * P::REC + 15) & ~size_t(15);
-  b += sizeof(double) * (size_t)P::G * P::CH * NP * 2;
-  b += sizeof(double) * (size_t)P::CH * NP * 2;
-  b += sizeof(EngineShared<2>) + 16;
-  return b;
+  return engine_smem_bytes<3, 2, GammaPolicy<R>>();
 }
 
 constexpr int GAMMA_NT = 256;

@@ -74,6 +74,10 @@ struct Map3Launch {
   unsigned* diag;    // device counter of bulk-copy timeouts (may be null)
 };
 
+// shared memory that the resident CTAs of k_map3<float> hold on one SM
+// (dynamic + per-block reserved)
+cudaError_t map3_f32_resident_smem(size_t* bytes);
+
 // grid size, dynamic shared memory and scratch bytes of a Map3 launch
 cudaError_t plan_map3(int precision, int njobs, int cap, int max_ctas, int* grid, size_t* smem, size_t* scratch);
 cudaError_t launch_map3(const Map3Launch& L, int grid, size_t smem, char* scratch, cudaStream_t st);

@@ -357,6 +357,19 @@ static cudaError_t plan_map3_t(int njobs, int cap, int max_ctas, int* grid, size
   return cudaSuccess;
 }
 
+cudaError_t map3_f32_resident_smem(size_t* bytes) {
+  const size_t smem = map3_smem_bytes<float>();
+  cudaError_t e =
+      cudaFuncSetAttribute(k_map3<float, MAP3_NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  int dev = 0, per_sm = 0, reserved = 0;
+  cudaGetDevice(&dev);
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_map3<float, MAP3_NT>, MAP3_NT, smem);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, dev);
+  *bytes = (size_t)per_sm * (smem + (size_t)reserved);
+  return e;
+}
+
 cudaError_t plan_map3(int precision, int njobs, int cap, int max_ctas, int* grid, size_t* smem, size_t* scratch) {
   return precision == TP_FP64 ? plan_map3_t<double>(njobs, cap, max_ctas, grid, smem, scratch)
                               : plan_map3_t<float>(njobs, cap, max_ctas, grid, smem, scratch);

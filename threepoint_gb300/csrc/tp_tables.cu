@@ -9,6 +9,7 @@
 
 #include "tp_bispec.cuh"
 #include "tp_internal.cuh"
+#include "tp_kernels.cuh"
 #include "tp_tables.cuh"
 
 namespace tp {
@@ -289,9 +290,6 @@ __device__ double d_lgr(const CosmoDev& c, double z) {
 #define TP_TABLES_MAXNREG 32
 #endif
 #define TP_TABLE_KERNEL __global__ void __maxnreg__(TP_TABLES_MAXNREG)
-#ifndef TP_RSIGMA_SMEM
-#define TP_RSIGMA_SMEM 8192
-#endif
 
 // norm = sigma8 / sigma(8 Mpc/h, top hat) and the growth integral at z = 0;
 // one warp per cosmology
@@ -705,9 +703,25 @@ cudaError_t build_tables(const CosmoDev* d_cos, EHConst* d_eh, const double* d_n
   // different kernels together only in one shared-memory/L1 configuration:
   // these kernels ask for the one k_map3 runs in (maximum shared memory).
   static thread_local int carveout_set = -1;
+  static thread_local size_t rsigma_smem = 0;
   int dev = 0;
   cudaGetDevice(&dev);
   if (carveout_set != dev) {
+    // k_rsigma (FP64-pipe bound) asks for shared memory it does not use: just
+    // over half of what the resident k_map3<float> CTAs leave free on an SM,
+    // so that one k_rsigma warp runs beside them instead of four (one per
+    // sub-partition by registers) and contends less with k_map3's own FP64
+    // instructions; alone it still fills the SM
+    size_t used = 0;
+    int smem_sm = 0, reserved = 0;
+    if (map3_f32_resident_smem(&used) == cudaSuccess &&
+        cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev) == cudaSuccess &&
+        cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, dev) == cudaSuccess) {
+      const long free_b = (long)smem_sm - (long)used;
+      rsigma_smem = free_b >= 2L * reserved + 2 ? (size_t)(free_b / 2 + 1) : 0;
+      if (rsigma_smem > 48 * 1024) rsigma_smem = 48 * 1024;
+    }
+    cudaGetLastError();  // a failed query leaves rsigma_smem = 0
     const void* ks[] = {(const void*)k_eh_table, (const void*)k_norm, (const void*)k_fk, (const void*)k_g, (const void*)k_growth,
                         (const void*)k_rsigma, (const void*)k_node_coefs, (const void*)k_finish,
                         (const void*)k_plin_table};
@@ -720,12 +734,7 @@ cudaError_t build_tables(const CosmoDev* d_cos, EHConst* d_eh, const double* d_n
   k_fk<<<n * (NZ / 32), 32, 0, s>>>(d_cos, d_tab, n);
   k_g<<<n * (NZ / 32), 32, 0, s>>>(d_cos, d_nz, nz_stride, d_tab, n);
   k_growth<<<n * (NZ / 32), 32, 0, s>>>(d_cos, d_tab, n);
-  // k_rsigma (FP64-pipe bound) also takes TP_RSIGMA_SMEM bytes of shared
-  // memory it does not use: beside three k_map3 CTAs, which leave ~15 KB of an
-  // SM's shared memory, that admits one of its warps per SM instead of four,
-  // so it contends less with k_map3's own FP64 instructions; alone it still
-  // fills the SM
-  k_rsigma<<<(unsigned)((long)n * (NZ / RS_BINS)), 32, TP_RSIGMA_SMEM, s>>>(d_cos, d_eh, d_tab, d_ehg, n);
+  k_rsigma<<<(unsigned)((long)n * (NZ / RS_BINS)), 32, rsigma_smem, s>>>(d_cos, d_eh, d_tab, d_ehg, n);
   k_node_coefs<<<n * (NNODE / 32), 32, 0, s>>>(d_cos, d_tab, d_ncoef, d_ncoef_f, d_fcoef_f, d_hcoef, d_hcoef_f, n);
   k_finish<<<n, 32, 0, s>>>(d_cos, d_eh, d_tab, d_ncoef, d_ncoef_f, d_fcoef_f, d_wscale64, d_wscale32, d_ck64, d_ck32,
                             n);
