@@ -40,7 +40,7 @@ N_LHS = 4096
 # ncu dram__bytes_read.sum + dram__bytes_write.sum of a 880-integral launch
 # (4 LHS cosmologies x 220 triplets: 65.9 + 221.5 MB); the region-store
 # traffic grows with the number of integrals
-TRAFFIC_PER_INTEGRAL = (65.906176e6 + 221.541888e6) / 880
+TRAFFIC_PER_INTEGRAL = (70.184192e6 + 225.050112e6) / 880
 SFU_PER_NODE = 22  # SFU ops (ex2/rcp.approx) per line-of-sight node of the FP32 BiHalofit evaluation (NF_* rows, merged reciprocals)
 NNODE = 96
 
