@@ -263,6 +263,44 @@ int tp_likelihood_chi2(tp_likelihood* lk, const double* models, int n_models, do
 int tp_likelihood_chi2_device(tp_likelihood* lk, const double* models_device, int n_models, long ld,
                               double* chi2_device, void* stream);
 
+/* ---- surrogate network of log b_kappa ----------------------------------- */
+
+/* A multilayer perceptron 8 -> 256 -> 256 -> 256 -> 256 -> 1 (SiLU after the
+ * hidden layers, linear output) on the tensor cores: BF16 operands, FP32
+ * accumulation, FP32 master parameters and Adam moments. It has no
+ * counterpart in the reference; its inputs are the 8 scaled features of a
+ * (triangle, cosmology) point and its output the scaled log b_kappa
+ * (threepoint_gb300/surrogate.py defines the scaling). Parameters travel as
+ * one flat FP64 array: W1 [256][8], b1 [256], W2, W3, W4 [256][256] with their
+ * biases, W5 [1][256], b5 [1] (tp_mlp_param_count() values; W[out][in]).
+ * Loss: mean squared error. Every call runs on the network's own stream;
+ * max_batch bounds one forward / gradient / training batch. */
+typedef struct tp_mlp tp_mlp;
+long tp_mlp_param_count(void);
+int tp_mlp_create(int device, int max_batch, tp_mlp** out);
+void tp_mlp_destroy(tp_mlp* m);
+const char* tp_mlp_last_error(const tp_mlp* m);
+int tp_mlp_set_params(tp_mlp* m, const double* params);
+int tp_mlp_get_params(tp_mlp* m, double* params);
+/* y[n] for features x[n][8] (host buffers; any n, in batches of max_batch) */
+int tp_mlp_forward(tp_mlp* m, const double* x, long n, double* y);
+/* loss and its gradient (flat, the parameter layout) on one batch, no update */
+int tp_mlp_gradients(tp_mlp* m, const double* x, const double* t, long n, double* grads, double* loss);
+/* one Adam step (Kingma & Ba 2015, beta 0.9 / 0.999, eps 1e-8) on one batch in
+ * device memory (x [n][8], t [n], FP32); asynchronous; *loss_dev (device,
+ * optional) receives the batch's loss before the update */
+int tp_mlp_train_step_device(tp_mlp* m, const float* x_dev, const float* t_dev, long n, float lr,
+                             float* loss_dev);
+/* waits for the network's stream; TP_ERR_CUDA if a kernel's tensor-core wait
+ * reached its iteration limit */
+int tp_mlp_sync(tp_mlp* m);
+void* tp_mlp_stream(const tp_mlp* m);
+/* C = A B^T on the tensor cores (device pointers, the network's stream): A
+ * [M][lda], B [N][ldb] BF16 with K contiguous, C [M][ldc] FP32; M % 128 == 0,
+ * N % 32 == 0 with 32 <= N <= 256, K % 64 == 0, lda and ldb multiples of 8 */
+int tp_gemm_bf16_device(tp_mlp* m, const void* A, int lda, const void* B, int ldb, float* C, int ldc, int M, int N,
+                        int K);
+
 #ifdef __cplusplus
 }
 #endif

@@ -178,6 +178,22 @@ def lib():
         L.tp_likelihood_cov_inv.argtypes = [p, dp]
         L.tp_likelihood_chi2.argtypes = [p, dp, i, dp]
         L.tp_likelihood_chi2_device.argtypes = [p, p, i, l, p, p]
+        L.tp_mlp_param_count.restype = l
+        L.tp_mlp_param_count.argtypes = []
+        L.tp_mlp_create.argtypes = [i, i, C.POINTER(p)]
+        L.tp_mlp_destroy.argtypes = [p]
+        L.tp_mlp_destroy.restype = None
+        L.tp_mlp_last_error.argtypes = [p]
+        L.tp_mlp_last_error.restype = C.c_char_p
+        L.tp_mlp_set_params.argtypes = [p, dp]
+        L.tp_mlp_get_params.argtypes = [p, dp]
+        L.tp_mlp_forward.argtypes = [p, dp, l, dp]
+        L.tp_mlp_gradients.argtypes = [p, dp, dp, l, dp, dp]
+        L.tp_mlp_train_step_device.argtypes = [p, p, p, l, C.c_float, p]
+        L.tp_mlp_sync.argtypes = [p]
+        L.tp_mlp_stream.argtypes = [p]
+        L.tp_mlp_stream.restype = p
+        L.tp_gemm_bf16_device.argtypes = [p, p, i, p, i, p, i, i, i, i]
         _lib = L
     return _lib
 
@@ -475,6 +491,110 @@ class Likelihood:
     def close(self):
         if self._h:
             lib().tp_likelihood_destroy(self._h)
+            self._h = C.c_void_p(0)
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class MLP:
+    """The b_kappa surrogate network (8 -> 256 x 4 -> 1, SiLU) on the tensor
+    cores: BF16 operands, FP32 accumulation and master parameters, Adam.
+
+    Parameters are a list [(W [out, in], b [out])] of five layers, or the flat
+    FP64 array of the C ABI (tp_mlp_param_count() values)."""
+
+    WIDTHS = (8, 256, 256, 256, 256, 1)
+
+    def __init__(self, max_batch=65536, device=0):
+        self._h = C.c_void_p(0)
+        self.device = device
+        self.max_batch = max_batch
+        st = lib().tp_mlp_create(device, max_batch, C.byref(self._h))
+        if st != TP_OK:
+            msg = lib().tp_mlp_last_error(self._h).decode() if self._h else ""
+            self.close()
+            raise ThreepointError(st, msg)
+
+    @staticmethod
+    def param_count():
+        return int(lib().tp_mlp_param_count())
+
+    @classmethod
+    def flatten(cls, params):
+        return np.concatenate([np.concatenate([np.asarray(W, dtype=np.float64).reshape(-1),
+                                               np.asarray(b, dtype=np.float64).reshape(-1)]) for W, b in params])
+
+    @classmethod
+    def unflatten(cls, flat):
+        out, o = [], 0
+        for i in range(len(cls.WIDTHS) - 1):
+            fi, fo = cls.WIDTHS[i], cls.WIDTHS[i + 1]
+            W = flat[o:o + fi * fo].reshape(fo, fi)
+            o += fi * fo
+            out.append((W, flat[o:o + fo].copy()))
+            o += fo
+        return out
+
+    def set_params(self, params):
+        flat = params if isinstance(params, np.ndarray) and params.ndim == 1 else self.flatten(params)
+        flat = _arr(flat)
+        if flat.size != self.param_count():
+            raise ValueError(f"{flat.size} parameters for {self.param_count()}")
+        self._chk(lib().tp_mlp_set_params(self._h, _dp(flat)))
+
+    def get_params(self, flat=False):
+        out = np.zeros(self.param_count())
+        self._chk(lib().tp_mlp_get_params(self._h, _dp(out)))
+        return out if flat else self.unflatten(out)
+
+    def forward(self, x):
+        x = _arr(x).reshape(-1, 8)
+        y = np.zeros(len(x))
+        self._chk(lib().tp_mlp_forward(self._h, _dp(x), len(x), _dp(y)))
+        return y
+
+    def gradients(self, x, t):
+        """(loss, [(dW, db)]) of the mean squared error on one batch"""
+        x = _arr(x).reshape(-1, 8)
+        t = _arr(t).reshape(-1)
+        g = np.zeros(self.param_count())
+        loss = C.c_double(0)
+        self._chk(lib().tp_mlp_gradients(self._h, _dp(x), _dp(t), len(x), _dp(g), C.byref(loss)))
+        return loss.value, self.unflatten(g)
+
+    def train_step_device(self, x, t, lr, loss_out=None):
+        """x: CUDA float32 [n, 8], t: [n]; asynchronous on self.stream_handle"""
+        self._chk(lib().tp_mlp_train_step_device(self._h, C.c_void_p(x.data_ptr()), C.c_void_p(t.data_ptr()),
+                                                 int(t.numel()), float(lr),
+                                                 C.c_void_p(loss_out.data_ptr()) if loss_out is not None else None))
+
+    def sync(self):
+        self._chk(lib().tp_mlp_sync(self._h))
+
+    @property
+    def stream_handle(self):
+        return lib().tp_mlp_stream(self._h)
+
+    def gemm_device(self, A, B, Cout):
+        """Cout = A B^T on the tensor cores (torch CUDA tensors: A, B bfloat16
+        [M, K], [N, K] row-major; Cout float32 [M, N])"""
+        M, K = A.shape
+        N = B.shape[0]
+        self._chk(lib().tp_gemm_bf16_device(self._h, C.c_void_p(A.data_ptr()), int(A.stride(0)),
+                                            C.c_void_p(B.data_ptr()), int(B.stride(0)), C.c_void_p(Cout.data_ptr()),
+                                            int(Cout.stride(0)), int(M), int(N), int(K)))
+
+    def _chk(self, st):
+        if st != TP_OK:
+            raise ThreepointError(st, lib().tp_mlp_last_error(self._h).decode())
+
+    def close(self):
+        if self._h:
+            lib().tp_mlp_destroy(self._h)
             self._h = C.c_void_p(0)
 
     def __del__(self):
