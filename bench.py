@@ -344,7 +344,9 @@ def run_ours(args):
                    "table_build_ms_alone": statistics.mean(build_ms), "map3_ms_alone": statistics.mean(map3_ms),
                    "job_order": "none" if args.no_order else "longest-first by warm-up cost per triplet",
                    "max_rel_err_fp32_vs_fp64": max_rel, "fp64_check_integrals": int(v64.size),
-                   "zero_valued_agree": zeros_agree},
+                   "zero_valued_agree": zeros_agree,
+                   "integrand": "FP32 line-of-sight BiHalofit (96 nodes, packed pairs) at every point; "
+                                "the b_kappa surrogate network is not used in this line"},
         "e2e": {"value": e2e_val, "unit": "triplets/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": 10 * args.steps,  # 9 table-build kernels + k_map3 per step
         "roofline": {"bound": "sfu", "achieved": achieved / 1e9, "peak": sfu_peak / 1e9, "unit": "Gop/s",
