@@ -277,6 +277,7 @@ int tp_likelihood_chi2_device(tp_likelihood* lk, const double* models_device, in
  * max_batch bounds one forward / gradient / training batch. */
 typedef struct tp_mlp tp_mlp;
 long tp_mlp_param_count(void);
+/* on failure *out is NULL (TP_ERR_ARG: max_batch outside [1, 2^22]) */
 int tp_mlp_create(int device, int max_batch, tp_mlp** out);
 void tp_mlp_destroy(tp_mlp* m);
 const char* tp_mlp_last_error(const tp_mlp* m);

@@ -515,9 +515,8 @@ class MLP:
         self.max_batch = max_batch
         st = lib().tp_mlp_create(device, max_batch, C.byref(self._h))
         if st != TP_OK:
-            msg = lib().tp_mlp_last_error(self._h).decode() if self._h else ""
-            self.close()
-            raise ThreepointError(st, msg)
+            self._h = C.c_void_p(0)
+            raise ThreepointError(st, f"tp_mlp_create(device={device}, max_batch={max_batch}) failed")
 
     @staticmethod
     def param_count():

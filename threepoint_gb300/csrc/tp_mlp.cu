@@ -615,6 +615,8 @@ static cudaError_t mlp_upload_x(tp_mlp* m, const double* x, long n, int rows) {
 
 extern "C" long tp_mlp_param_count(void) { return P_COUNT; }
 
+extern "C" void tp_mlp_destroy(tp_mlp* m);
+
 extern "C" int tp_mlp_create(int device, int max_batch, tp_mlp** out) {
   if (!out || max_batch < 1 || max_batch > (1 << 22)) return TP_ERR_ARG;
   *out = nullptr;
@@ -659,8 +661,7 @@ extern "C" int tp_mlp_create(int device, int max_batch, tp_mlp** out) {
   if (e == cudaSuccess) e = cudaMemsetAsync(m->d_err, 0, sizeof(unsigned), m->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(m->stream);
   if (e != cudaSuccess) {
-    m->err = std::string("mlp create: ") + cudaGetErrorString(e);
-    *out = m;  // the caller reads the error, then destroys
+    tp_mlp_destroy(m);
     return TP_ERR_CUDA;
   }
   *out = m;
