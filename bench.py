@@ -531,6 +531,85 @@ def run_cov(args):
             "fp64": {"pairs": n64, "seconds_per_term": t64, "rel_err_fp32_vs_fp64": err}}
 
 
+def run_surrogate(args):
+    """The b_kappa surrogate network of config 4: FP64 line-of-sight targets
+    for --sg-cosmo Latin-hypercube cosmologies x --sg-points triangles each
+    (2^24 points by default), Adam on the tensor-core network, the relative
+    error of b_kappa on --sg-holdout other cosmologies, the forward rate of the
+    host API, and the roofline of the GEMM every layer runs (65536 x 256 x 256,
+    BF16, against the measured cuBLAS BF16 peak)."""
+    import torch
+
+    import threepoint_gb300 as tp
+    from threepoint_gb300 import surrogate as S
+
+    rank, world, local = dist_env()
+    if rank != 0:
+        return None
+    torch.cuda.set_device(local)
+    zs, ns = nz_config()
+    nz = tp.rebin_n_of_z(zs, ns, 256, 3.0)
+    cos = S.lhs_box(args.sg_cosmo + args.sg_holdout, seed=LHS_SEED + 4)
+    ctx = tp.Context(local)
+    t0 = time.perf_counter()
+    x, y = S.generate(ctx, cos[:args.sg_cosmo], nz, args.sg_points, seed=1)
+    t_gen = time.perf_counter() - t0
+    xh, yh = S.generate(ctx, cos[args.sg_cosmo:], nz, args.sg_holdout_points, seed=2)
+    ctx.close()
+    sg = S.Surrogate(max_batch=args.sg_batch, device=local, seed=0)
+    t0 = time.perf_counter()
+    hist = sg.fit(x, y, steps=args.sg_steps, batch=args.sg_batch, lr=args.sg_lr, lr_end=args.sg_lr * 1e-2,
+                  log_every=max(1, args.sg_steps // 10))
+    t_train = time.perf_counter() - t0
+    held = sg.evaluate(xh, yh)
+    train_sample = sg.evaluate(x[:65536], y[:65536])
+    t0 = time.perf_counter()
+    sg.net.forward(xh)
+    t_fwd = time.perf_counter() - t0
+
+    # GEMM roofline: CUDA events on the network's stream around each launch
+    Mg, Ng, Kg = 65536, 256, 256
+    g = torch.Generator().manual_seed(0)
+    A = torch.randn(Mg, Kg, generator=g).to(torch.bfloat16).cuda()
+    B = torch.randn(Ng, Kg, generator=g).to(torch.bfloat16).cuda()
+    Cm = torch.empty(Mg, Ng, dtype=torch.float32, device="cuda")
+    st = torch.cuda.ExternalStream(sg.net.stream_handle, device=local)
+    for _ in range(3):
+        sg.net.gemm_device(A, B, Cm)
+    times = []
+    for _ in range(20):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        sg.net.gemm_device(A, B, Cm)
+        e1.record(st)
+        torch.cuda.synchronize()
+        times.append(e0.elapsed_time(e1) * 1e-3)
+    t_gemm = statistics.median(times)
+    tflops = 2.0 * Mg * Ng * Kg / t_gemm / 1e12
+    peak, src = 1900.0, "fallback 1.9 PFLOP/s"
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peak, src = float(json.load(f)["bf16_tflops"]), "MEASURED_PEAKS.json bf16_tflops (cuBLAS burst)"
+    except Exception:
+        pass
+    sg.close()
+    return {"metric": "b_kappa surrogate (config 4): held-out relative error of b_kappa, forward points/s",
+            "value": len(yh) / t_fwd, "unit": "points/s", "n_gpus": 1, "steps": args.sg_steps, "warmup": 0,
+            "ms_per_step": t_train / max(1, args.sg_steps) * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "bf16", "data": "synthetic",
+            "config": {"workload": f"{args.sg_cosmo} LHS cosmologies x {args.sg_points} triangles (l1, l2 "
+                                   f"log-uniform on [10, 4e4], l3 in range), FP64 line-of-sight targets; "
+                                   f"{args.sg_holdout} held-out cosmologies x {args.sg_holdout_points}",
+                       "network": "8-256-256-256-256-1 SiLU, BF16 operands, FP32 accumulation and master weights",
+                       "optimizer": f"Adam, batch {args.sg_batch}, lr {args.sg_lr:g} -> {args.sg_lr * 1e-2:g}",
+                       "value_timing": "host API tp_mlp_forward over the held-out points (copies included)"},
+            "accuracy": {"held_out": held, "train_sample": train_sample},
+            "training": {"points": int(len(y)), "generation_s": t_gen, "train_s": t_train, "loss_history": hist},
+            "roofline": {"bound": "tensor", "achieved": tflops, "peak": peak, "unit": "TFLOP/s", "frac": tflops / peak,
+                         "traffic": None, "kernel": f"k_gemm_tc {Mg} x {Ng} x {Kg}", "peak_source": src,
+                         "ms_per_launch": t_gemm * 1e3}}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -546,13 +625,21 @@ def main():
     ap.add_argument("--no-order", action="store_true")
     ap.add_argument("--no-fp64-plain", action="store_true", help="skip the plain FP64 comparison run")
     ap.add_argument("--no-pipeline", action="store_true", help="one context, steps run one after another")
-    ap.add_argument("--workload", default="map3", choices=["map3", "gamma", "cov"],
-                    help="map3: the headline metric; gamma / cov: the shear-3PCF grid and covariance configurations")
+    ap.add_argument("--workload", default="map3", choices=["map3", "gamma", "cov", "surrogate"],
+                    help="map3: the headline metric; gamma / cov: the shear-3PCF grid and covariance "
+                         "configurations; surrogate: training and accuracy of the b_kappa network")
     ap.add_argument("--gamma-triangles", type=int, default=0, help="first N triangles of the grid (0 = all 1000)")
     ap.add_argument("--gamma-fp64-sample", type=int, default=20)
     ap.add_argument("--cov-pairs", type=int, default=24)
     ap.add_argument("--cov-fp64-pairs", type=int, default=4)
     ap.add_argument("--cov-terms", default="T1,T2,T4", help="comma-separated subset of T1,T2,T4")
+    ap.add_argument("--sg-cosmo", type=int, default=64)
+    ap.add_argument("--sg-points", type=int, default=1 << 18, help="training triangles per cosmology")
+    ap.add_argument("--sg-holdout", type=int, default=8)
+    ap.add_argument("--sg-holdout-points", type=int, default=1 << 14)
+    ap.add_argument("--sg-steps", type=int, default=20000)
+    ap.add_argument("--sg-batch", type=int, default=65536)
+    ap.add_argument("--sg-lr", type=float, default=2e-3)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
     if args.impl == "reference":
@@ -561,6 +648,8 @@ def main():
         res = run_gamma(args)
     elif args.workload == "cov":
         res = run_cov(args)
+    elif args.workload == "surrogate":
+        res = run_surrogate(args)
     else:
         res = run_ours(args)
     if res is not None:
