@@ -259,12 +259,14 @@ def run_ours(args):
     # outside the timed region
     timings = []
     live_total = 0
+    neval_total = 0
     n_roof = min(args.steps, 3)
     for s in range(n_roof):
         torch.cuda.synchronize()
         one_step(args.warmup + s, 0, timings, flush_first=True)
         torch.cuda.synchronize()
         live_total += int(nlive.sum().item())
+        neval_total += int(nev.sum().item())
         if args.dump_costs and s == 0:
             np.savez(args.dump_costs, theta=np.tile(th, (C, 1)), neval=nev.cpu().numpy(), nlive=nlive.cpu().numpy(),
                      value=out.cpu().numpy())
@@ -355,6 +357,7 @@ def run_ours(args):
                      "peak_source": "measured now by tp_pipe_peaks (ex2.approx.f32 loop, whole device)",
                      "kernel": "k_map3<float>", "kernel_ms_per_launch": map3_avg_s * 1e3,
                      "fp32_fma_peak_tflops": f32_peak / 1e12, "fp64_fma_peak_tflops": f64_peak / 1e12},
+        "reference_work": reference_work(neval_total / n_roof, map3_avg_s),
         "clocks": clocks,
         "plain_fp64_gpu": None if fp64_val is None else {
             "value": fp64_val, "unit": "triplets/s", "integrals": n64, "fp32_speedup": value / fp64_val,
@@ -364,6 +367,22 @@ def run_ours(args):
     if not args.no_cpu_baseline:
         res["cpu_baseline"] = cpu_baseline(args, sample_triplets=args.cpu_sample)
     return res
+
+
+def reference_work(points_per_launch, launch_s):
+    """The launch's work in operations of the reference's FP64 formula chain:
+    evaluated cubature points x the counted operations of one point
+    (roofline.json, oracle/opcount.py; transcendental calls weighted as stated
+    there). The GPU path folds most of that chain into per-cosmology tables, so
+    this rate measures useful work, not the GPU's own instruction rate."""
+    try:
+        with open(os.path.join(ROOT, "roofline.json")) as f:
+            per_point = float(json.load(f)["map3_point"]["flop_equivalent"])
+    except (OSError, KeyError, ValueError):
+        return None
+    return {"flop_equivalent_per_point": per_point, "points_per_launch": points_per_launch,
+            "achieved_tflop_equivalent_per_s": points_per_launch * per_point / launch_s / 1e12,
+            "source": "roofline.json (oracle/opcount.py)"}
 
 
 def cpu_baseline(args, sample_triplets=2):
