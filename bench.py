@@ -550,6 +550,66 @@ def run_cov(args):
             "fp64": {"pairs": n64, "seconds_per_term": t64, "rel_err_fp32_vs_fp64": err}}
 
 
+def run_plain(args):
+    """The plain form (FP64 BiHalofit, FP64 cubature) on the fiducial
+    cosmology and the 20 triplets of radii {2, 4, 8, 16}', through the host
+    API, at the reference's l bound [1, 10/theta_min] and at the configuration's
+    [1, 1e5]; the FP32 path beside it, and the CPU oracle on a sample of the
+    same triplets."""
+    import torch
+
+    import threepoint_gb300 as tp
+
+    rank, world, local = dist_env()
+    if rank != 0:
+        return None
+    torch.cuda.set_device(local)
+    zs, ns = nz_config()
+    nz = tp.rebin_n_of_z(zs, ns, 256, 3.0)
+    ctx = tp.Context(local)
+    ctx.set_cosmology(tp.cosmology(**COSMO_FID), nz)
+    r = np.array([2.0, 4.0, 8.0, 16.0]) * ARCMIN
+    th = np.array([(r[i], r[j], r[k]) for i in range(4) for j in range(i, 4) for k in range(j, 4)])
+    out = {}
+    vals = {}
+    for name, prec in (("fp64", tp.FP64), ("fp32", tp.FP32)):
+        for lname, lmax in (("l_ref", 0.0), ("l_1e5", 1e5)):
+            ctx.map3_batch(th[:1], precision=prec, lMax=lmax, check=False)  # warm-up
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            v = ctx.map3_batch(th, precision=prec, lMax=lmax, check=False)
+            dt = time.perf_counter() - t0
+            vals[(name, lname)] = v[0]
+            out[f"{name}_{lname}"] = {"value": len(th) / dt, "unit": "triplets/s", "seconds": dt}
+    ctx.close()
+    for lname in ("l_ref", "l_1e5"):
+        a, b = vals[("fp32", lname)], vals[("fp64", lname)]
+        nzm = b != 0
+        out[f"fp32_{lname}"]["max_rel_err_vs_fp64"] = float(np.max(np.abs(a[nzm] - b[nzm]) / np.abs(b[nzm])))
+    l_shift = vals[("fp64", "l_1e5")] / vals[("fp64", "l_ref")] - 1.0
+    res = {"metric": "plain <Map^3> FP64 triplets/s (fiducial cosmology, 20 triplets of {2,4,8,16} arcmin)",
+           "value": out["fp64_l_ref"]["value"], "unit": "triplets/s", "n_gpus": 1, "steps": 1, "warmup": 1,
+           "ms_per_step": out["fp64_l_ref"]["seconds"] * 1e3, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+           "config": {"workload": "fiducial flat wCDM, n(z) ~ z^2 exp(-(z/0.5)^1.5), 20 triplets, rel 1e-4",
+                      "timing": "host API tp_map3_batch (copies included)"},
+           "lines": out, "fp64_l_1e5_vs_l_ref_max_rel": float(np.max(np.abs(l_shift[np.isfinite(l_shift)])))}
+    if not args.no_cpu_baseline:
+        import oracle
+
+        n = os.cpu_count() or 1
+        oracle.set_threads(n)
+        T = oracle.Tables(COSMO_FID, oracle.read_n_of_z(zs, ns, 256, 3.0))
+        pick = th[:: max(1, len(th) // 2)][:2]
+        t0 = time.perf_counter()
+        for t in pick:
+            T.map3(list(t))
+        dt = time.perf_counter() - t0
+        res["cpu_baseline"] = {"value": len(pick) / dt, "unit": "triplets/s", "cores": n, "kind": "port",
+                               "sample": f"{len(pick)} of the 20 triplets, FP64, {n} threads, l in [1, 10/theta_min]"}
+    return res
+
+
 def run_surrogate(args):
     """The b_kappa surrogate network of config 4: FP64 line-of-sight targets
     for --sg-cosmo Latin-hypercube cosmologies x --sg-points triangles each
@@ -644,9 +704,10 @@ def main():
     ap.add_argument("--no-order", action="store_true")
     ap.add_argument("--no-fp64-plain", action="store_true", help="skip the plain FP64 comparison run")
     ap.add_argument("--no-pipeline", action="store_true", help="one context, steps run one after another")
-    ap.add_argument("--workload", default="map3", choices=["map3", "gamma", "cov", "surrogate"],
+    ap.add_argument("--workload", default="map3", choices=["map3", "gamma", "cov", "surrogate", "plain"],
                     help="map3: the headline metric; gamma / cov: the shear-3PCF grid and covariance "
-                         "configurations; surrogate: training and accuracy of the b_kappa network")
+                         "configurations; surrogate: training and accuracy of the b_kappa network; plain: the "
+                         "FP64 form on the fiducial 20 triplets")
     ap.add_argument("--gamma-triangles", type=int, default=0, help="first N triangles of the grid (0 = all 1000)")
     ap.add_argument("--gamma-fp64-sample", type=int, default=20)
     ap.add_argument("--cov-pairs", type=int, default=24)
@@ -669,6 +730,8 @@ def main():
         res = run_cov(args)
     elif args.workload == "surrogate":
         res = run_surrogate(args)
+    elif args.workload == "plain":
+        res = run_plain(args)
     else:
         res = run_ours(args)
     if res is not None:
