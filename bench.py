@@ -468,6 +468,8 @@ def run_gamma(args):
         return None
     torch.cuda.set_device(local)
     ctx = tp.Context(local)
+    if args.gamma_region_cap != 32768:
+        ctx.set_limits(args.gamma_region_cap)
     zs, ns = nz_config()
     ctx.set_cosmology(tp.cosmology(**COSMO_FID), tp.rebin_n_of_z(zs, ns, 256, 3.0))
     cfg = tp.configGamma(10, 10, 10, 0.0, 1.0, -1.0, 1.0, 0.1, 100.0)
@@ -710,6 +712,8 @@ def main():
                          "FP64 form on the fiducial 20 triplets")
     ap.add_argument("--gamma-triangles", type=int, default=0, help="first N triangles of the grid (0 = all 1000)")
     ap.add_argument("--gamma-fp64-sample", type=int, default=20)
+    ap.add_argument("--gamma-region-cap", type=int, default=32768,
+                    help="regions per Gamma integral (the grid's small triangles need more than the default)")
     ap.add_argument("--cov-pairs", type=int, default=24)
     ap.add_argument("--cov-fp64-pairs", type=int, default=4)
     ap.add_argument("--cov-terms", default="T1,T2,T4", help="comma-separated subset of T1,T2,T4")
