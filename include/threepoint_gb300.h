@@ -139,7 +139,13 @@ int tp_pipe_peaks(int device, double* out);
  *   nz: 256 values per cosmology (nz_stride = 256) or one shared row
  *       (nz_stride = 0), as produced by tp_read_n_of_z.
  *   pk: optional (NULL -> Eisenstein & Hu): 256 log-spaced linear P(k) values
- *       per cosmology with dk, kmin, kmax as from convert_Pk (helpers.cu:202-214). */
+ *       per cosmology with dk, kmin, kmax as from convert_Pk (helpers.cu:202-214).
+ *       As in the reference, the table is read only by the bispectrum's and
+ *       P(ell)'s linear P(k) (bispectrum.cu:605-621); the sigma_8
+ *       normalisation and the non-linear scales r_sigma, n_eff, ncur still
+ *       come from Eisenstein & Hu, because the reference's set_cosmology
+ *       declares a local Pk_given (:132) that hides the global flag its host
+ *       code reads (:36, :623). */
 int tp_set_cosmologies(tp_ctx* ctx, const tp_cosmology* cosmo, int n_cosmo, const double* nz, int nz_stride,
                        const double* pk, double dk, double kmin, double kmax);
 
@@ -165,6 +171,23 @@ int tp_bkappa_batch(tp_ctx* ctx, const int* cosmo_index, const double* ell, long
 
 /* Pell(ell) (cuda_version/bispectrum.cu:511-529, device branch) for n values. */
 int tp_pell_batch(tp_ctx* ctx, int cosmo_index, const double* ell, long n, int precision, double* out);
+
+/* The 96 line-of-sight terms of bkappa (GQ96_of_bdelta, cuda_version/bispectrum.cu:293-309)
+ * for n triangles ell[n][3] of one cosmology, evaluated by the functions the
+ * integration kernels use: term[i*96 + j] = W96 * z_max/2 * 27/8 Om^3 (H0/c)^5 *
+ * integrand_bkappa(z_j, ell) (:311-333) at Gauss node j (j even: z_max/2 (1 - a_{j/2}),
+ * odd: z_max/2 (1 + a_{j/2})), so a triangle's terms sum to bkappa; bispec
+ * (optional, same shape) receives bispec(ell/f_K(z_j), z_j) (:221-291). */
+int tp_bkappa_nodes(tp_ctx* ctx, int cosmo_index, const double* ell, long n, int precision, double* term,
+                    double* bispec);
+
+/* The Gamma cubature integrand at n points pts[n][3] = (z, phi, psi) of the
+ * triangle x[3] (radians): out[2i], out[2i+1] = real and imaginary part of the
+ * sum over the Ogata nodes k = 1..32 of full_integrand_gamma0 (which = 0) or
+ * full_integrand_gamma1 (which = 1) (cuda_version/gamma.cu:267-363, 419-482),
+ * before the cubature and the outer prefactor. */
+int tp_gamma_integrand_points(tp_ctx* ctx, int cosmo_index, const double* x, int which, const double* pts, int n,
+                              int precision, double* out);
 
 /* ---- adaptive integrals ------------------------------------------------- */
 
@@ -201,9 +224,11 @@ int tp_map3_jobs_device(tp_ctx* ctx, const int* job_cosmo_device, const double* 
  * in pipelines that forbid allocation after start-up): it calls no cudaMalloc
  * or cudaFree and keeps the per-CTA region stores in a fixed 128 MiB
  * __device__ array of the library (held on every GPU that loads the library
- * until exit). Limits: at most 8192 regions per integral (an integral that
- * needs more stops with status != 0 and TP_ERR_CAPACITY is reported through
- * status_device) and a grid trimmed to fit the array. The first call on a
+ * until exit). Limits: at most 8192 regions per integral and a grid trimmed
+ * to fit the array (192 CTAs). An integral that needs more regions stops at
+ * the cap with bit 1 set in its status_device entry (bit 2: not converged
+ * within the sweep limit) and its value still written; the call itself
+ * returns TP_OK then, not TP_ERR_CAPACITY. The first call on a
  * device looks up the array's device address (cudaGetSymbolAddress): make it
  * before any stream capture. All calls share the array, so calls that overlap
  * on the GPU race; serialise them. Inputs, outputs and the context's

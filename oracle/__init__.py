@@ -87,6 +87,7 @@ def lib():
         L.orc_ogata_weights.argtypes = [dp]
         L.orc_gamma.argtypes = [p, i, d, d, d, d, d, dp, dp, C.POINTER(l)]
         L.orc_ggg_analytic.argtypes = [d, d, d, dp, dp]
+        L.orc_gamma_integrand_points.argtypes = [p, i, d, d, d, dp, l, dp]
         cp = C.POINTER(CovParams)
         L.orc_T1.restype = d
         L.orc_T1.argtypes = [p, cp, dp, d, C.POINTER(l)]
@@ -251,6 +252,14 @@ class Tables:
         nev = C.c_long(0)
         lib().orc_gamma(self._h, comp, x1, x2, x3, rel, abs_tol, C.byref(re), C.byref(im), C.byref(nev))
         return complex(re.value, im.value), nev.value
+
+    def gamma_integrand_points(self, which, x1, x2, x3, pts):
+        """Sum over the Ogata nodes of the Gamma^0 (which=0) or Gamma^1
+        (which=1) integrand at points (z, phi, psi); complex array."""
+        pts = np.ascontiguousarray(pts, dtype=np.float64).reshape(-1, 3)
+        out = np.zeros(2 * len(pts))
+        lib().orc_gamma_integrand_points(self._h, which, x1, x2, x3, _dp(pts), len(pts), _dp(out))
+        return out[0::2] + 1j * out[1::2]
 
     def cov_T(self, term, params: CovParams, th6, rel=0.0):
         th = np.array(th6, dtype=np.float64)

@@ -901,14 +901,13 @@ extern "C" orc_tables* orc_tables_create(const orc_cosmo* c, const double* nz, c
                                          double kmin, double kmax) {
   orc_tables* t = new orc_tables();
   t->c = *c;
-  if (pk) {
-    t->pk_given = true;
-    std::memcpy(t->pk, pk, sizeof(double) * NK);
-    t->dk = dk;
-    t->kmin = kmin;
-    t->kmax = kmax;
-  }
-  // set_cosmology, bispectrum.cu:148-212
+  // set_cosmology, bispectrum.cu:148-212. With a given P(k) the reference
+  // still builds norm, r_sigma, n_eff and ncur from Eisenstein & Hu: its
+  // set_cosmology declares a local `bool Pk_given` (bispectrum.cu:132) that
+  // shadows the global flag the host linear_pk reads (:36, :623), and the
+  // host Pk/dk/k_min/k_max globals are never filled. Only the device-side
+  // linear_pk (dev_Pk_given, :605-621) reads the table. So the table is
+  // attached after the build.
   t->norm = 1;
   t->norm = t->c.sigma8 / sigmam(t, 8., 0);
   t->z_max = t->c.zmax;
@@ -935,6 +934,13 @@ extern "C" orc_tables* orc_tables_create(const orc_cosmo* c, const double* nz, c
     double d1 = -2. * pow(t->D1[i] * s2, 2);
     t->n_eff[i] = -3. + 2. * pow(t->D1[i] * s2, 2);
     t->ncur[i] = d1 * d1 + 4. * sigmam(t, t->r_sigma[i], 3) * pow(t->D1[i], 2);
+  }
+  if (pk) {
+    t->pk_given = true;
+    std::memcpy(t->pk, pk, sizeof(double) * NK);
+    t->dk = dk;
+    t->kmin = kmin;
+    t->kmax = kmax;
   }
   return t;
 }
@@ -1261,6 +1267,17 @@ extern "C" void orc_gamma(const orc_tables* t, int comp, double x1, double x2, d
   r = r * 27. / 8. * pow(t->c.om, 3) * pow(100. / 299792., 5) / 3. / (2 * pow(2 * PI, 3));
   *re = r.real();
   *im = r.imag();
+}
+
+// The Gamma cubature integrand at given points (z, phi, psi): the sum over the
+// Ogata nodes k = 1 .. prec_k-1 of full_integrand_gamma0 (which = 0) or
+// full_integrand_gamma1 (which = 1), as compute_integrand_gamma0/1 form it
+// per point (gamma.cu:267-363); out[2i], out[2i+1] = real, imaginary part.
+extern "C" void orc_gamma_integrand_points(const orc_tables* t, int which, double x1, double x2, double x3,
+                                           const double* pts, long n, double* out) {
+  (void)ogata();
+  GammaCtx g{t, which, x1, x2, x3};
+  integrand_gamma_v(3, (size_t)n, pts, &g, 2, out);
 }
 
 // closed-form Gamma^0 for the analytic test bispectrum,

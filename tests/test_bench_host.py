@@ -22,7 +22,7 @@ def test_reference_work_reads_roofline_json():
         per_point = json.load(f)["map3_point"]["flop_equivalent"]
     r = b.reference_work(2.0e9, 1.2)
     assert r["flop_equivalent_per_point"] == per_point
-    assert abs(r["achieved_tflop_equivalent_per_s"] - 2.0e9 * per_point / 1.2 / 1e12) < 1e-9
+    assert abs(r["tflop_equivalent_per_s"] - 2.0e9 * per_point / 1.2 / 1e12) < 1e-9
 
 
 def test_every_workload_parses():
@@ -38,3 +38,19 @@ def test_workload_helpers():
     assert len(b.thetas_220()) == 220
     cs = b.lhs_cosmologies(16, seed=1)
     assert len(cs) == 16 and all(abs(c["om"] - c["omb"] - c["omc"]) < 1e-15 for c in cs)
+
+
+def test_output_errors_and_corners():
+    import numpy as np
+
+    bench = load_bench()
+    v64 = np.array([1.0, 2.0, 0.0, -4.0])
+    v32 = np.array([1.0005, 2.0, 0.0, -4.0])
+    r = bench.output_errors(v32, v64)
+    assert r["outputs"] == 4 and r["nonzero_outputs"] == 3 and r["zero_valued_agree"]
+    assert abs(r["max_rel"] - 5e-4) < 1e-12 and r["outputs_above_1e-3"] == 0
+    assert not bench.output_errors(np.array([1e-30, 1.0]), np.array([0.0, 1.0]))["zero_valued_agree"]
+    cs = bench.corner_cosmologies()
+    assert len(cs) == 4
+    for key, lo, hi in (("om", 0.2, 0.4), ("sigma8", 0.7, 0.9), ("h", 0.6, 0.8), ("w", -1.2, -0.8), ("ns", 0.92, 1.0)):
+        assert {c[key] for c in cs} == {lo, hi}, key

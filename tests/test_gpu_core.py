@@ -192,3 +192,37 @@ def test_bkappa_on_reference_dump_grid(gpu_ctx, oracle_tables):
     got32 = gpu_ctx.bkappa(ell, precision=1)
     rel32 = np.abs(got32[nz] - ref[nz]) / np.abs(ref[nz])
     assert np.median(rel32) < 1e-5 and rel32.max() < 1e-3, (np.median(rel32), rel32.max())
+
+
+def test_bkappa_nodes_sum_to_bkappa_and_match_oracle(gpu_ctx, oracle_tables):
+    """tp_bkappa_nodes: the 96 line-of-sight terms of a triangle sum to
+    tp_bkappa_batch's b_kappa, and each term equals the oracle's
+    integrand_bkappa at that node times the Gauss weight and prefactor."""
+    ell = random_triangles(16, seed=5, lmin=10.0, lmax=4e4)
+    a, w = O.gq96()
+    z = np.empty(96)
+    z[0::2], z[1::2] = 1.5 - 1.5 * a, 1.5 + 1.5 * a
+    wq = np.repeat(w * 1.5, 2)
+    pref = 27.0 / 8.0 * COSMO1["om"] ** 3 * (100.0 / 299792.0) ** 5
+    for prec, tol_sum, tol_node in ((0, 1e-12, 1e-10), (1, 1e-5, 1e-3)):
+        term, bis = gpu_ctx.bkappa_nodes(ell, 0, precision=prec)
+        tot = gpu_ctx.bkappa(ell, precision=prec)
+        assert np.max(np.abs(term.sum(1) - tot) / np.abs(tot)) < tol_sum
+        ref = np.array([[oracle_tables.integrand_bkappa(zz, *e) * wq[j] * pref for j, zz in enumerate(z)]
+                        for e in ell])
+        # g(z) vanishes at the last nodes before z_max: those terms are exactly 0
+        nzm = ref != 0
+        assert np.all(np.abs(term[~nzm]) <= 1e-12 * np.abs(ref).max())
+        r = np.abs(term[nzm] - ref[nzm]) / np.abs(ref[nzm])
+        assert np.median(r) < tol_node * 1e-2 and r.max() < tol_node, (prec, np.median(r), r.max())
+
+
+def test_gamma_integrand_points_match_oracle(gpu_ctx, oracle_tables):
+    rng = np.random.default_rng(11)
+    pts = np.stack([rng.uniform(0.01, 2.99, 32), rng.uniform(0, 2 * np.pi, 32), rng.uniform(0.01, 1.56, 32)], 1)
+    x = np.array([4.0, 6.0, 8.0]) * ARC
+    for which in (0, 1):
+        ref = oracle_tables.gamma_integrand_points(which, *x, pts)
+        for prec, tol in ((0, 1e-10), (1, 1e-3)):
+            got = gpu_ctx.gamma_integrand_points(which, x, pts, precision=prec)
+            assert np.max(np.abs(got - ref)) < tol * np.max(np.abs(ref)), (which, prec)

@@ -33,7 +33,7 @@ def setup(nz256):
     ctx.close()
 
 
-def _run(torch, tp, ctx, fn_name, th, precision):
+def _run(torch, tp, ctx, fn_name, th, precision, rel_tol=1e-4):
     dev = torch.device("cuda", 0)
     n = len(th)
     jc = torch.zeros(n, dtype=torch.int32, device=dev)
@@ -42,7 +42,7 @@ def _run(torch, tp, ctx, fn_name, th, precision):
     err = torch.zeros(n, dtype=torch.float64, device=dev)
     st = torch.full((n,), -1, dtype=torch.int32, device=dev)
     L = tp.lib()
-    args = (ctx._h, _ptr(jc), _ptr(jt), n, 0.0, 2 * math.pi, 1.0, 0.0, 1e-4, precision)
+    args = (ctx._h, _ptr(jc), _ptr(jt), n, 0.0, 2 * math.pi, 1.0, 0.0, rel_tol, precision)
     if fn_name == "noalloc":
         rc = L.tp_map3_jobs_noalloc(*args, _ptr(out), _ptr(err), _ptr(st))
     else:
@@ -65,3 +65,17 @@ def test_noalloc_matches_regular_entry_point_twice(setup, precision):
         got, st = _run(torch, tp, ctx, "noalloc", th, precision)
         assert np.all(st == 0)
         assert np.allclose(got, ref, rtol=1e-12, atol=0), (got, ref)
+
+
+def test_noalloc_region_cap_sets_status_bit(setup):
+    """An integral that needs more than the entry point's 8192 regions stops
+    at the cap: bit 1 of its status is set, its value is still written and the
+    call itself returns success."""
+    torch, tp, ctx = setup
+    th = [[2 * ARC, 2 * ARC, 2 * ARC], [16 * ARC, 16 * ARC, 16 * ARC]]
+    got, st = _run(torch, tp, ctx, "noalloc", th, 1, rel_tol=1e-9)
+    assert st[0] & 1, st
+    assert np.all(np.isfinite(got))
+    ref, st_ref = _run(torch, tp, ctx, "regular", th[:1], 1)
+    assert st_ref[0] == 0
+    assert abs(got[0] / ref[0] - 1) < 1e-3

@@ -155,6 +155,8 @@ def lib():
         L.tp_get_tables.argtypes = [p, i, dp]
         L.tp_bkappa_batch.argtypes = [p, ip, dp, l, i, dp]
         L.tp_pell_batch.argtypes = [p, i, dp, l, i, dp]
+        L.tp_bkappa_nodes.argtypes = [p, i, dp, l, i, dp, dp]
+        L.tp_gamma_integrand_points.argtypes = [p, i, dp, i, dp, i, i, dp]
         L.tp_map3_batch.argtypes = [p, ip, i, dp, i, d, d, d, d, d, i, dp, dp, i64p, ip]
         L.tp_map3_jobs_device.argtypes = [p, p, p, i, d, d, d, d, d, i, p, p, p, p, p, p]
         L.tp_ctx_set_limits.argtypes = [p, i, i]
@@ -334,6 +336,26 @@ class Context:
             ip = ci.ctypes.data_as(C.POINTER(C.c_int))
         _check(self._h, lib().tp_bkappa_batch(self._h, ip, _dp(ell), len(ell), precision, _dp(out)))
         return out
+
+    def bkappa_nodes(self, ell, cosmo_index=0, precision=FP64):
+        """The 96 line-of-sight terms of bkappa per triangle (they sum to
+        bkappa) and the bispectrum at each node: two [n][96] arrays."""
+        ell = _arr(ell).reshape(-1, 3)
+        term = np.zeros((len(ell), 96))
+        bis = np.zeros((len(ell), 96))
+        _check(self._h, lib().tp_bkappa_nodes(self._h, cosmo_index, _dp(ell), len(ell), precision, _dp(term),
+                                              _dp(bis)))
+        return term, bis
+
+    def gamma_integrand_points(self, which, x, pts, cosmo_index=0, precision=FP64):
+        """The Gamma^0 (which=0) or Gamma^1 (which=1) cubature integrand of
+        triangle x at points (z, phi, psi), summed over the Ogata nodes."""
+        x = _arr(x).reshape(3)
+        pts = _arr(pts).reshape(-1, 3)
+        out = np.zeros(2 * len(pts))
+        _check(self._h, lib().tp_gamma_integrand_points(self._h, cosmo_index, _dp(x), which, _dp(pts), len(pts),
+                                                        precision, _dp(out)))
+        return out[0::2] + 1j * out[1::2]
 
     def Pell(self, ell, cosmo_index=0, precision=FP64):
         ell = _arr(ell).reshape(-1)

@@ -534,6 +534,33 @@ extern "C" int tp_bkappa_batch(tp_ctx* ctx, const int* cosmo_index, const double
   return tp_cuda(ctx, e, "bkappa");
 }
 
+extern "C" int tp_bkappa_nodes(tp_ctx* ctx, int cosmo_index, const double* ell, long n, int precision, double* term,
+                               double* bispec) {
+  TpRange nvtx_range("tp_bkappa_nodes");
+  if (!ctx || !ell || !term || n < 0) return TP_ERR_ARG;
+  if (precision != TP_FP64 && precision != TP_FP32) return TP_ERR_ARG;
+  if (cosmo_index < 0 || cosmo_index >= ctx->n_cosmo) return tp_fail(ctx, TP_ERR_STATE, "no such cosmology");
+  if (n == 0) return TP_OK;
+  cudaSetDevice(ctx->device);
+  const size_t b_ell = sizeof(double) * 3 * n, b_node = sizeof(double) * NNODE * n;
+  const size_t o_t = (b_ell + 255) & ~size_t(255), o_b = o_t + ((b_node + 255) & ~size_t(255));
+  int st = ctx->ensure_io(o_b + b_node + 256);
+  if (st) return st;
+  char* base = ctx->d_io;
+  cudaStream_t s = ctx->stream;
+  cudaError_t e = cudaMemcpyAsync(base, ell, b_ell, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess)
+    e = launch_bkappa_nodes(precision, cosmo_index, (const double*)base, n,
+                            precision == TP_FP64 ? (const void*)ctx->d_ncoef64 : (const void*)ctx->d_fcoef32,
+                            precision == TP_FP64 ? ctx->d_wscale64 : ctx->d_wscale32,
+                            precision == TP_FP64 ? ctx->d_ck64 : ctx->d_ck32, (double*)(base + o_t),
+                            bispec ? (double*)(base + o_b) : nullptr, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(term, base + o_t, b_node, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess && bispec) e = cudaMemcpyAsync(bispec, base + o_b, b_node, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  return tp_cuda(ctx, e, "bkappa nodes");
+}
+
 // ---------------------------------------------------------------------------
 // <Map^3>
 // ---------------------------------------------------------------------------

@@ -81,7 +81,7 @@ struct Slot {
   int* pend;      // [cap]
   uint8_t* split; // [cap]
   int cap;
-  __host__ __device__ static size_t bytes(int cap) {
+  __host__ __device__ static constexpr size_t bytes(int cap) {
     return (size_t)cap * (sizeof(double) * (2 * DIM + 2 + 2 * FDIM) + sizeof(int) + 1) + 256;
   }
   __device__ void init(char* base, int c) {

@@ -340,6 +340,31 @@ __global__ void __launch_bounds__(NT, sizeof(R) == 4 ? TP_GAMMA_MINB : 1) k_gamm
   adaptive_body<3, 2, NT, GammaPolicy<R>>(pol, njobs, job_counter, cfg, scratch, slot_bytes);
 }
 
+// The Gamma integrand at caller-given points (no cubature): the policy's
+// point set-up and its node groups, summed over the groups, one thread per
+// point; dynamic shared memory GammaPolicy<R>::PSMEM.
+template <typename R>
+__global__ void k_gamma_points(GammaPolicy<R> pol, const double* pts, int n, double* out) {
+  extern __shared__ __align__(16) char psmem_[];
+  double xmin[3], xmax[3];
+  pol.begin_job(0, psmem_, xmin, xmax);
+  for (int p = threadIdx.x; p < n; p += blockDim.x) {
+    alignas(16) char rec[GammaPolicy<R>::REC];
+    double sum[2] = {0.0, 0.0}, fv[2];
+    if (pol.setup(p, pts + 3 * p, rec)) {
+      for (int g = 0; g < GammaPolicy<R>::G; ++g) {
+        double pv[2];
+        pol.group(rec, g, pv);
+        sum[0] += pv[0];
+        sum[1] += pv[1];
+      }
+    }
+    pol.finalize(rec, sum, fv);
+    out[2 * p] = fv[0];
+    out[2 * p + 1] = fv[1];
+  }
+}
+
 template <typename R>
 static size_t gamma_smem_bytes() {
   return engine_smem_bytes<3, 2, GammaPolicy<R>>();
@@ -398,6 +423,61 @@ extern "C" int tp_ogata_weights(double* out) {
     out[3 * PREC_K + k] = k == 0 ? NAN : o.prod[1][k];
   }
   return TP_OK;
+}
+
+extern "C" int tp_gamma_integrand_points(tp_ctx* ctx, int cosmo_index, const double* x, int which, const double* pts,
+                                         int n, int precision, double* out) {
+  TpRange nvtx_range("tp_gamma_integrand_points");
+  if (!ctx || !x || !pts || !out || n < 0 || (which != 0 && which != 1)) return TP_ERR_ARG;
+  if (precision != TP_FP64 && precision != TP_FP32) return TP_ERR_ARG;
+  if (cosmo_index < 0 || cosmo_index >= ctx->n_cosmo) return tp_fail(ctx, TP_ERR_STATE, "no such cosmology");
+  if (!(x[0] > 0 && x[1] > 0 && x[2] > 0)) return tp_fail(ctx, TP_ERR_ARG, "triangle sides must be > 0");
+  if (n == 0) return TP_OK;
+  cudaSetDevice(ctx->device);
+  cudaError_t e = gamma_upload_constants();
+  if (e != cudaSuccess) return tp_cuda(ctx, e, "ogata constants");
+  const int jc[2] = {which, 0};  // job 0: component `which` of triangle 0
+  const size_t o_c = 256, o_p = 512, o_o = o_p + ((sizeof(double) * 3 * n + 255) & ~size_t(255));
+  int st = ctx->ensure_io(o_o + sizeof(double) * 2 * n + 256);
+  if (st) return st;
+  char* b = ctx->d_io;
+  cudaStream_t s = ctx->stream;
+  e = cudaMemcpyAsync(b, x, sizeof(double) * 3, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(b + o_c, jc, sizeof(jc), cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(b + o_p, pts, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, s);
+  if (e != cudaSuccess) return tp_cuda(ctx, e, "gamma points upload");
+  const int nt = 128;
+  if (precision == TP_FP64) {
+    GammaPolicy<double> pol;
+    pol.J.x = (const double*)b;
+    pol.J.comp = (const int*)(b + o_c);
+    pol.J.tri = (const int*)(b + o_c) + 1;
+    pol.tab = ctx->d_tab;
+    pol.cosm = ctx->d_cos;
+    pol.ck = (const CosmoK<double>*)ctx->d_ck64;
+    pol.cosmo = cosmo_index;
+    pol.out = nullptr;
+    pol.status = nullptr;
+    k_gamma_points<double><<<1, nt, GammaPolicy<double>::PSMEM, s>>>(pol, (const double*)(b + o_p), n,
+                                                                      (double*)(b + o_o));
+  } else {
+    GammaPolicy<float> pol;
+    pol.J.x = (const double*)b;
+    pol.J.comp = (const int*)(b + o_c);
+    pol.J.tri = (const int*)(b + o_c) + 1;
+    pol.tab = ctx->d_tab;
+    pol.cosm = ctx->d_cos;
+    pol.ck = (const CosmoK<float>*)ctx->d_ck32;
+    pol.cosmo = cosmo_index;
+    pol.out = nullptr;
+    pol.status = nullptr;
+    k_gamma_points<float><<<1, nt, GammaPolicy<float>::PSMEM, s>>>(pol, (const double*)(b + o_p), n,
+                                                                    (double*)(b + o_o));
+  }
+  e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaMemcpyAsync(out, b + o_o, sizeof(double) * 2 * n, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  return tp_cuda(ctx, e, "gamma points");
 }
 
 extern "C" int tp_gamma_batch(tp_ctx* ctx, int cosmo_index, const double* x, int n, int comp_mask, double rel_tol,

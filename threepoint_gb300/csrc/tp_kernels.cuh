@@ -84,5 +84,7 @@ cudaError_t launch_map3(const Map3Launch& L, int grid, size_t smem, char* scratc
 
 cudaError_t launch_bkappa_points(int precision, const int* cosmo_idx, const double* ell, long n, const void* ncoef,
                                  const double* wscale, const void* ck, double* out, cudaStream_t st);
+cudaError_t launch_bkappa_nodes(int precision, int cosmo, const double* ell, long n, const void* ncoef,
+                                const double* wscale, const void* ck, double* term, double* bis, cudaStream_t st);
 
 }  // namespace tp

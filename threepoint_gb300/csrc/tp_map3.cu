@@ -333,6 +333,79 @@ __global__ void k_bkappa_points(const int* cosmo_idx, const double* ell, long n,
   if (lane == 0) out[w] = s * wscale[c];
 }
 
+// Per-node terms of b_kappa at given triangles (no cubature), with the
+// functions of the integration kernels: term[i * NNODE + j] is node j's
+// line-of-sight term of triangle i (Gauss weight, 27/8 Om^3 (H0/c)^5 and
+// (g(1+z))^3 / f_K / E(z) included, NaN -> 0 as integrand_bkappa does,
+// bispectrum.cu:311-333), so that the terms of a triangle sum to b_kappa;
+// bis (optional) is B(ell / f_K(z_j), z_j) itself (bispec, :221-291).
+// FP64: one thread per (triangle, node), bispec_eval on the NC_* rows. FP32:
+// one thread per (triangle, node pair), the packed pair evaluation of k_map3
+// (merged reciprocals, and the separate-reciprocal form with the per-node
+// zeroing when a merged product leaves the float range).
+template <typename R>
+__global__ void k_bkappa_nodes(int c, const double* ell, long n, const R* node_coef, const double* wscale,
+                               const CosmoK<R>* ck, double* term, double* bis) {
+  constexpr int PER = sizeof(R) == 4 ? NNODE / 2 : NNODE;
+  const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n * PER) return;
+  const long i = t / PER;
+  const int u = (int)(t % PER);
+  const double l1 = ell[3 * i], l2 = ell[3 * i + 1], l3 = ell[3 * i + 2];
+  const int j0 = sizeof(R) == 4 ? 2 * u : u, nj = sizeof(R) == 4 ? 2 : 1;
+  if (!(l1 > 1e-10 && l2 > 1e-10 && l3 > 1e-10)) {
+    for (int q = 0; q < nj; ++q) {
+      term[i * NNODE + j0 + q] = 0.0;
+      if (bis) bis[i * NNODE + j0 + q] = 0.0;
+    }
+    return;
+  }
+  const R* nc = node_coef + (size_t)c * NCP * NNODE;
+  const CosmoK<R> K = ck[c];
+  Tri<R> T;
+  make_tri<R>(l1, l2, l3, T);
+  if constexpr (sizeof(R) == 4) {
+    TriF F;
+    trif_from_tri(T, F);
+    const float2* cp = reinterpret_cast<const float2*>(nc) + (size_t)u * NCP;
+    float2 B = bispec_pair<TriF, true>(cp, F, K);
+    float2 v = p2mul(cp[NF_W], B);
+    if (!isfinite(v.x + v.y)) {
+      B = bispec_pair<TriF, false>(cp, F, K);
+      v = p2mul(cp[NF_W], B);
+      if (v.x != v.x) v.x = 0.f;
+      if (v.y != v.y) v.y = 0.f;
+    }
+    term[i * NNODE + j0] = (double)v.x * wscale[c];
+    term[i * NNODE + j0 + 1] = (double)v.y * wscale[c];
+    if (bis) {
+      bis[i * NNODE + j0] = (double)B.x;
+      bis[i * NNODE + j0 + 1] = (double)B.y;
+    }
+  } else {
+    const R* row = nc + (size_t)u * NCP;
+    const R B = bispec_eval<R>(row, 1, row[NC_S], row[NC_L2S], row[NC_HF], row[NC_L2HF], T, K);
+    R v = row[NC_W] * B;
+    if (v != v) v = (R)0;
+    term[i * NNODE + u] = (double)v * wscale[c];
+    if (bis) bis[i * NNODE + u] = (double)B;
+  }
+}
+
+cudaError_t launch_bkappa_nodes(int precision, int cosmo, const double* ell, long n, const void* ncoef,
+                                const double* wscale, const void* ck, double* term, double* bis, cudaStream_t st) {
+  const long per = precision == TP_FP64 ? NNODE : NNODE / 2;
+  const int bs = 192;
+  const unsigned grid = (unsigned)((n * per + bs - 1) / bs);
+  if (precision == TP_FP64)
+    k_bkappa_nodes<double><<<grid, bs, 0, st>>>(cosmo, ell, n, (const double*)ncoef, wscale,
+                                                 (const CosmoK<double>*)ck, term, bis);
+  else
+    k_bkappa_nodes<float><<<grid, bs, 0, st>>>(cosmo, ell, n, (const float*)ncoef, wscale,
+                                                (const CosmoK<float>*)ck, term, bis);
+  return cudaGetLastError();
+}
+
 // ---------------------------------------------------------------------------
 constexpr int MAP3_NT = 256;
 

@@ -16,16 +16,20 @@
 // state that must start at zero, the job counter, is cleared by each call.
 #include <cuda_runtime.h>
 
+#include <mutex>
 #include <string>
 
 #include "tp_capi_internal.h"
 #include "tp_cubature.cuh"
 #include "tp_kernels.cuh"
 
-// 128 MiB: 188 CTAs of 8192-region stores for the 3-D <Map^3> integrals
+// 128 MiB: 192 CTAs of 8192-region stores (696,576 bytes each) for the 3-D
+// <Map^3> integrals
 #define TP_NOALLOC_SCRATCH_BYTES (128u << 20)
 #define TP_NOALLOC_REGION_CAP 8192
 #define TP_NOALLOC_MAX_DEVICES 64
+static_assert(TP_NOALLOC_SCRATCH_BYTES / tp::Slot<3, 1>::bytes(TP_NOALLOC_REGION_CAP) == 192,
+              "the array holds 192 region stores of the cap");
 
 static __device__ __align__(256) char g_noalloc_scratch[TP_NOALLOC_SCRATCH_BYTES];
 static __device__ __align__(256) int g_noalloc_counter[64];
@@ -38,10 +42,14 @@ struct NoallocDevice {
 };
 NoallocDevice g_dev[TP_NOALLOC_MAX_DEVICES];
 
+std::mutex g_setup_mutex;
+
 // Once per device, with that device current: the host-side names of the
 // __device__ arrays are only stand-ins, so their device addresses are looked
-// up here and passed to the kernel.
+// up here and passed to the kernel. First calls from two host threads are
+// serialised by the mutex.
 int noalloc_setup(tp_ctx* ctx) {
+  std::lock_guard<std::mutex> lock(g_setup_mutex);
   NoallocDevice& d = g_dev[ctx->device];
   if (d.ready) return TP_OK;
   void* p = nullptr;
@@ -110,7 +118,7 @@ extern "C" int tp_map3_jobs_noalloc(tp_ctx* ctx, const int* job_cosmo_device, co
   L.nlive = nullptr;
   L.status = status_device;
   L.job_counter = d.counter;  // cleared by launch_map3 (cudaMemsetAsync) before the kernel
-  L.diag = nullptr;
+  L.diag = ctx->d_diag;  // allocated with the context: bulk-copy timeouts are counted as in tp_map3_jobs_device
   L.job_order = nullptr;
   e = launch_map3(L, grid, smem, d.scratch, ctx->stream);
   return tp_cuda(ctx, e, "no-alloc map3 launch");

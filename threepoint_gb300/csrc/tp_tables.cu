@@ -291,12 +291,24 @@ __device__ double d_lgr(const CosmoDev& c, double z) {
 #endif
 #define TP_TABLE_KERNEL __global__ void __maxnreg__(TP_TABLES_MAXNREG)
 
+// The table build reads the Eisenstein & Hu P(k) even when a linear P(k)
+// table is given, as the reference does: its set_cosmology declares a local
+// Pk_given (cuda_version/bispectrum.cu:132) that shadows the global flag its
+// host linear_pk reads (:36, :623), so norm, r_sigma, n_eff and ncur come from
+// Eisenstein & Hu and only the bispectrum's linear P(k) reads the table
+// (dev_Pk_given, :605-621). tables_cosmo() is the cosmology the build sees.
+__device__ __forceinline__ CosmoDev tables_cosmo(const CosmoDev& in) {
+  CosmoDev c = in;
+  c.pk_given = 0;
+  return c;
+}
+
 // norm = sigma8 / sigma(8 Mpc/h, top hat) and the growth integral at z = 0;
 // one warp per cosmology
 TP_TABLE_KERNEL k_norm(const CosmoDev* cos, EHConst* eh, TablesDev* tab, int n) {
   int ci = blockIdx.x;
   if (ci >= n) return;
-  CosmoDev c = cos[ci];
+  const CosmoDev c = tables_cosmo(cos[ci]);
   EHConst e = eh[ci];  // built with norm = 1
   double s = warp_sigmam(c, e, tab[ci].pk, 8., 0);
   if (threadIdx.x == 0) {
@@ -350,7 +362,7 @@ TP_TABLE_KERNEL k_growth(const CosmoDev* cos, TablesDev* tab, int n) {
 TP_TABLE_KERNEL k_eh_table(const CosmoDev* cos, const EHConst* eh, double* ehg, int n) {
   const long idx = (long)blockIdx.x * blockDim.x + threadIdx.x;
   const int ci = (int)(idx / EHG_N), i = (int)(idx % EHG_N);
-  if (ci >= n || cos[ci].pk_given) return;
+  if (ci >= n) return;
   const double t = EHG_T0 + i / EHG_PER_UNIT;
   ehg[(size_t)ci * EHG_N + i] = 2.0 * log(eh_transfer(eh[ci], exp(t)));
 }
@@ -372,7 +384,7 @@ TP_TABLE_KERNEL k_rsigma(const CosmoDev* cos, const EHConst* eh, TablesDev* tab,
   const int ci = blockIdx.x / (NZ / RS_BINS), b0 = (blockIdx.x % (NZ / RS_BINS)) * RS_BINS;
   if (ci >= n) return;
   const int lane = threadIdx.x & 31;
-  const CosmoDev c = cos[ci];
+  const CosmoDev c = tables_cosmo(cos[ci]);
   const EHConst e = eh[ci];
   TablesDev& t = tab[ci];
   const double* pk = t.pk;
