@@ -503,9 +503,9 @@ def run_gamma(args):
     zs, ns = nz_config()
     ctx.set_cosmology(tp.cosmology(**COSMO_FID), tp.rebin_n_of_z(zs, ns, 256, 3.0))
     cfg = tp.configGamma(10, 10, 10, 0.0, 1.0, -1.0, 1.0, 0.1, 100.0)
-    x, _ = cfg.triangles()
+    x, ruv = cfg.triangles()
     n = len(x) if args.gamma_triangles <= 0 else min(len(x), args.gamma_triangles)
-    x = x[:n]
+    x, ruv = x[:n], ruv[:n]
     ctx.gamma_batch(x[: min(n, 8)], precision=tp.FP32)  # warm-up
     times = []
     for _ in range(args.steps):
@@ -513,11 +513,13 @@ def run_gamma(args):
         t0 = time.perf_counter()
         g32 = ctx.gamma_batch(x, precision=tp.FP32, check=False)
         times.append(time.perf_counter() - t0)
-        capped = int((ctx.last_gamma_status != 0).sum())
+        st32 = ctx.last_gamma_status.copy()
+        capped = int((st32 != 0).sum())
     sub = np.arange(0, n, max(1, n // args.gamma_fp64_sample))
     t0 = time.perf_counter()
     g64 = ctx.gamma_batch(x[sub], precision=tp.FP64, check=False)
     t64 = time.perf_counter() - t0
+    st64 = ctx.last_gamma_status.copy()
     err = _rel_stats(np.stack([g32[sub].real, g32[sub].imag]), np.stack([g64.real, g64.imag]))
     tot = sum(times)
     return {"metric": "Gamma_0..3 triangles/s (4 natural components, rel. tol 1e-3)", "value": n * args.steps / tot,
@@ -525,9 +527,10 @@ def run_gamma(args):
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": f"calculateGamma grid: {n} (r,u,v) bin centres x 4 components, fiducial cosmology",
                        "timing": "host API tp_gamma_batch per step (host inputs and outputs)",
-                       "triangles_at_cap": capped},
+                       "region_cap": args.gamma_region_cap, "triangles_at_cap": capped,
+                       "capped_r_u_v": [[round(float(v), 4) for v in ruv[i]] for i in np.nonzero(st32)[0][:200]]},
             "fp64": {"triangles": int(len(sub)), "triangles_per_s": len(sub) / t64,
-                     "rel_err_fp32_vs_fp64": err}}
+                     "triangles_at_cap": int((st64 != 0).sum()), "rel_err_fp32_vs_fp64": err}}
 
 
 def run_cov(args):

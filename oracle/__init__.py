@@ -91,6 +91,8 @@ def lib():
         cp = C.POINTER(CovParams)
         L.orc_T1.restype = d
         L.orc_T1.argtypes = [p, cp, dp, d, C.POINTER(l)]
+        L.orc_T1_capped.restype = d
+        L.orc_T1_capped.argtypes = [p, cp, dp, d, l, dp, C.POINTER(l)]
         L.orc_T2.restype = d
         L.orc_T2.argtypes = [p, cp, dp]
         L.orc_T4.restype = d

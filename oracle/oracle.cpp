@@ -1460,6 +1460,27 @@ extern "C" double orc_T1(const orc_tables* t, const orc_cov_params* p, const dou
   return res;
 }
 
+// The 6-D finite-field T1 of orc_T1 with an evaluation cap (maxEval, the
+// hcubature_v argument the reference passes as 0 = unbounded): the value and
+// error estimate reached after about maxEval integrand points, to measure how
+// far a configuration's integral is from the requested tolerance.
+extern "C" double orc_T1_capped(const orc_tables* t, const orc_cov_params* p, const double* th, double relTol,
+                                long maxEval, double* err_out, long* neval) {
+  double tmin123 = std::min({th[0], th[1], th[2]}), tmin456 = std::min({th[3], th[4], th[5]});
+  double lMax = 10. / std::max(tmin123, tmin456);
+  CovCtx c{t, p, {th[0], th[1], th[2], th[3], th[4], th[5]}, lMax};
+  double xmin[6], xmax[6], res = 0, err = 0;
+  for (int i = 0; i < 6; ++i) {
+    xmin[i] = -lMax;
+    xmax[i] = 1.02 * lMax;
+  }
+  orc_hcubature_v(1, integrand_T1_v, &c, 6, xmin, xmax, (size_t)maxEval, 0, relTol > 0 ? relTol : 1e-2, ORC_ERROR_L1,
+                  &res, &err);
+  if (neval) *neval = orc_last_neval();
+  if (err_out) *err_out = err / pow(2 * PI, 6);
+  return res / pow(2 * PI, 6);
+}
+
 // T2, apertureStatisticsCovariance.cu:1108-1164 (the 1-D upper bound is the
 // one computed from theta1..theta5 and is reused for the second 1-D integral)
 extern "C" double orc_T2(const orc_tables* t, const orc_cov_params* p, const double* th) {
