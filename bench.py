@@ -655,6 +655,105 @@ def run_plain(args):
     return res
 
 
+def apm_catalogue(n_gal, fieldsize, seed=7):
+    """Seeded synthetic shear catalogue: uniform positions on the field,
+    shears = a smooth large-scale pattern + shape noise sigma_eps = 0.3."""
+    rng = np.random.default_rng(seed)
+    x = rng.uniform(0.0, fieldsize, n_gal)
+    y = rng.uniform(0.0, fieldsize, n_gal)
+    g = 0.02 * np.exp(2j * np.pi * (x / 37.0 + y / 53.0)) + \
+        0.3 * (rng.standard_normal(n_gal) + 1j * rng.standard_normal(n_gal)) / np.sqrt(2)
+    return x, y, g
+
+
+def run_apm(args):
+    """The measurement side (python_scripts/aperture_mass_computer.py
+    extract_Map3): a shear catalogue of n_gal = 10 arcmin^-2 over a
+    240' x 240' field, CIC onto 4096^2 pixels, aperture-mass maps for
+    theta in {2, 4, 8, 16}' (exponential filter) and <Map^3> of the 20
+    triplets. One step = one field. `value` times the device-resident
+    pipeline (catalogue already in HBM), `e2e` the host API with the
+    catalogue copied in and the 20 values copied out every step."""
+    import torch
+
+    import threepoint_gb300 as tp
+    from threepoint_gb300 import aperture_mass as G
+
+    rank, world, local = dist_env()
+    if rank != 0:
+        return None
+    torch.cuda.set_device(local)
+    npix, fs, thetas = args.apm_npix, 240.0, [2.0, 4.0, 8.0, 16.0]
+    n_gal = int(10 * fs * fs)
+    x, y, g = apm_catalogue(n_gal, fs)
+    ctx = tp.Context(local)
+    plan = G._Plan(ctx, npix, fs, thetas, False)
+    dev = torch.device("cuda", local)
+    dx, dy = torch.tensor(x, device=dev), torch.tensor(y, device=dev)
+    d1, d2 = torch.tensor(g.real.copy(), device=dev), torch.tensor(g.imag.copy(), device=dev)
+    ntrip = len(thetas) * (len(thetas) + 1) * (len(thetas) + 2) // 6
+    out = torch.zeros(ntrip, dtype=torch.float64, device=dev)
+    st = torch.cuda.ExternalStream(ctx.stream_handle, device=local)
+    L = tp.lib()
+
+    def step():
+        rc = L.tp_apm_extract_map3_device(plan._h, dx.data_ptr(), dy.data_ptr(), d1.data_ptr(), d2.data_ptr(), n_gal,
+                                          1, out.data_ptr())
+        if rc:
+            raise RuntimeError(L.tp_last_error(ctx._h).decode())
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    sampler = ClockSampler(local)
+    sampler.start()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    for _ in range(args.steps):
+        step()
+    e1.record(st)
+    torch.cuda.synchronize()
+    clocks = sampler.stop()
+    t_dev = e0.elapsed_time(e1) * 1e-3
+    gpu_vals = out.cpu().numpy()
+    # e2e: host catalogue in, host results out, every step
+    t0 = time.perf_counter()
+    for _ in range(max(1, min(args.steps, 5))):
+        host = plan.extract_map3(x, y, g, True)
+    e2e_s = (time.perf_counter() - t0) / max(1, min(args.steps, 5))
+    res = {"metric": "<Map^3> fields/s (FFT aperture-mass measurement, extract_Map3)", "value": args.steps / t_dev,
+           "unit": "fields/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+           "ms_per_step": t_dev / args.steps * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+           "dtype": "f64", "data": "synthetic",
+           "config": {"workload": f"{n_gal} galaxies on a 240' field, CIC to {npix}^2, theta {thetas}', "
+                                  f"exponential filter, 20 triplets, same border for all",
+                      "fft_size": int(L.tp_apm_fft_size(plan._h)),
+                      "l2": "working set of several GB per field (> L2)"},
+           "e2e": {"value": 1.0 / e2e_s, "unit": "fields/s", "h2d_bytes_per_step": 4 * 8 * n_gal,
+                   "d2h_bytes_per_step": 8 * ntrip},
+           "gpu_launches": (6 + 2 * len(thetas)) * args.steps, "gpu_launches_note": "this library's kernels; cuFFT's transforms (3 + 2 per aperture per step) in addition", "clocks": clocks,
+           "device_vs_host_api_max_rel": float(np.max(np.abs(host - gpu_vals)) / np.max(np.abs(gpu_vals)))}
+    if not args.no_cpu_baseline:
+        from oracle import aperture_mass as A
+
+        # one aperture of the same field on the host (numpy/scipy, as the
+        # reference), the field time = gridding + 4 x that aperture's map
+        t0 = time.perf_counter()
+        grid, w = A.cic_grid(x, y, g, npix, fs)
+        t_grid = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        A.map_weighted(grid, w, A.q_grid(npix, fs, thetas[0]))
+        t_map = time.perf_counter() - t0
+        t_field = t_grid + len(thetas) * t_map
+        res["cpu_baseline"] = {"value": 1.0 / t_field, "unit": "fields/s", "cores": 1, "kind": "port",
+                               "sample": f"CIC gridding + 1 of the 4 aperture maps of the same field timed "
+                                         f"({t_grid:.2f} s + {t_map:.2f} s), field = gridding + 4 maps; "
+                                         f"numpy/scipy as the reference"}
+    plan.close()
+    ctx.close()
+    return res
+
+
 def run_surrogate(args):
     """The b_kappa surrogate network of config 4: FP64 line-of-sight targets
     for --sg-cosmo Latin-hypercube cosmologies x --sg-points triangles each
@@ -749,10 +848,11 @@ def main():
     ap.add_argument("--no-order", action="store_true")
     ap.add_argument("--no-fp64-plain", action="store_true", help="skip the plain FP64 comparison run")
     ap.add_argument("--no-pipeline", action="store_true", help="one context, steps run one after another")
-    ap.add_argument("--workload", default="map3", choices=["map3", "gamma", "cov", "surrogate", "plain"],
+    ap.add_argument("--apm-npix", type=int, default=4096, help="pixels per side of the aperture-mass grid")
+    ap.add_argument("--workload", default="map3", choices=["map3", "gamma", "cov", "surrogate", "plain", "apm"],
                     help="map3: the headline metric; gamma / cov: the shear-3PCF grid and covariance "
                          "configurations; surrogate: training and accuracy of the b_kappa network; plain: the "
-                         "FP64 form on the fiducial 20 triplets")
+                         "FP64 form on the fiducial 20 triplets; apm: the FFT aperture-mass measurement")
     ap.add_argument("--gamma-triangles", type=int, default=0, help="first N triangles of the grid (0 = all 1000)")
     ap.add_argument("--gamma-fp64-sample", type=int, default=20)
     ap.add_argument("--gamma-region-cap", type=int, default=32768,
@@ -779,6 +879,8 @@ def main():
         res = run_surrogate(args)
     elif args.workload == "plain":
         res = run_plain(args)
+    elif args.workload == "apm":
+        res = run_apm(args)
     else:
         res = run_ours(args)
     if res is not None:

@@ -247,6 +247,66 @@ int tp_map3_jobs_noalloc(tp_ctx* ctx, const int* job_cosmo_device, const double*
 int tp_gamma_batch(tp_ctx* ctx, int cosmo_index, const double* x, int n, int comp_mask, double rel_tol,
                    int precision, double* out, int* status_out);
 
+/* ---- FFT aperture-mass measurement ------------------------------------- */
+
+/* Replaces the reference's Python measurement side (python_scripts/
+ * aperture_mass_computer.py): class aperture_mass_computer(npix, theta_ap,
+ * fieldsize, use_polynomial_filter) (:19-372) and extract_Map3 /
+ * extract_Map3_of_field (:375-531). One tp_apm holds a grid of npix x npix
+ * pixels over a square field of side fieldsize, the n_theta aperture radii
+ * (fieldsize and thetas in the same unit, arcmin in the reference) and the
+ * filter (polynomial != 0: Schneider's polynomial filter, else the
+ * exponential one); it keeps on the device the Fourier transforms of the filter
+ * grids of every aperture, so only the field's own transforms are done per
+ * field. Needs cuFFT at run time (loaded with dlopen; TP_ERR_STATE if absent). */
+typedef struct tp_apm tp_apm;
+int tp_apm_create(tp_ctx* ctx, int npix, double fieldsize, const double* thetas, int n_theta, int polynomial,
+                  tp_apm** out);
+int tp_apm_destroy(tp_apm* apm);
+/* FFT grid side F >= 2 npix - 1 of the zero-padded convolutions */
+int tp_apm_fft_size(const tp_apm* apm);
+
+/* normalize_shear(Xs, Ys, shears, CIC=True, normalize=False) (:288-372):
+ * cloud-in-cell gridding of n_gal galaxies at (x, y) with shears g1 + i g2 on
+ * numpy.histogram2d's bins (edges i/(npix-1)*fieldsize); the shear-sum and
+ * weight grids stay in the tp_apm (row-major [x bin][y bin]). Host arrays; the
+ * _device form takes device arrays and does not synchronise. */
+int tp_apm_grid(tp_apm* apm, const double* x, const double* y, const double* g1, const double* g2, long n_gal);
+int tp_apm_grid_device(tp_apm* apm, const double* x_device, const double* y_device, const double* g1_device,
+                       const double* g2_device, long n_gal);
+/* set / read the gridded shear sums (re, im) and weights, npix*npix each */
+int tp_apm_set_grid(tp_apm* apm, const double* shear_re, const double* shear_im, const double* weight);
+int tp_apm_get_grid(tp_apm* apm, double* shear_re, double* shear_im, double* weight);
+
+/* Map_fft(gamma, norm=weights, normalize_weighted=True, periodic_boundary=False)
+ * (:199-286) for every aperture: maps[t][npix][npix] = (Im g * Im Q - Re g * Re Q)
+ * / (w * |Q|), '*' the zero-padded FFT convolution cropped to the grid
+ * (scipy.signal.fftconvolve 'same'); mcross (optional, return_mcross) =
+ * -(Re g * Im Q + Im g * Re Q) / (w * |Q|). Either output may be NULL. */
+int tp_apm_maps(tp_apm* apm, double* maps, double* mcross);
+
+/* Map_fft_from_kappa(kappa) (:183-197) for every aperture: maps[t] =
+ * fftconvolve(kappa, U_t, 'same') * fieldsize^2 / npix^2 with the exponential
+ * U filter (Ufunc, :72-80); kappa is npix*npix host values. The maps become
+ * the ones tp_apm_map3 reads. */
+int tp_apm_maps_from_kappa(tp_apm* apm, const double* kappa, double* maps);
+
+/* The <Map^3> part of extract_Map3_of_field (:466-531) over the maps of the
+ * last tp_apm_maps / extract call: out[q] for every triplet i <= j <= k of the
+ * apertures (in the order of the reference's loops) = the mean of
+ * M_i M_j M_k over [c, npix - c)^2, c = round(theta / fieldsize * npix * f)
+ * with f = 4 (exponential) or 1 (polynomial) and theta = theta_k, or the
+ * largest aperture when same_fieldsize != 0. */
+int tp_apm_map3(tp_apm* apm, int same_fieldsize, double* out);
+
+/* extract_Map3(Xs, Ys, shear_catalogue, npix, thetas, fieldsize) (:375-405):
+ * gridding, maps and <Map^3> in one call, host catalogue in, host results out;
+ * the _device form reads device arrays and writes out_device asynchronously. */
+int tp_apm_extract_map3(tp_apm* apm, const double* x, const double* y, const double* g1, const double* g2, long n_gal,
+                        int same_fieldsize, double* out);
+int tp_apm_extract_map3_device(tp_apm* apm, const double* x_device, const double* y_device, const double* g1_device,
+                               const double* g2_device, long n_gal, int same_fieldsize, double* out_device);
+
 /* Ogata nodes/weights of compute_weights_bessel (cuda_version/gamma.cu:13-56):
  * out[4][33] = psi(J6), product(J6), psi(J2), product(J2). */
 int tp_ogata_weights(double* out);

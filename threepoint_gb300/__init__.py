@@ -157,6 +157,18 @@ def lib():
         L.tp_pell_batch.argtypes = [p, i, dp, l, i, dp]
         L.tp_bkappa_nodes.argtypes = [p, i, dp, l, i, dp, dp]
         L.tp_gamma_integrand_points.argtypes = [p, i, dp, i, dp, i, i, dp]
+        L.tp_apm_create.argtypes = [p, i, d, dp, i, i, C.POINTER(p)]
+        L.tp_apm_destroy.argtypes = [p]
+        L.tp_apm_fft_size.argtypes = [p]
+        L.tp_apm_grid.argtypes = [p, dp, dp, dp, dp, l]
+        L.tp_apm_grid_device.argtypes = [p, p, p, p, p, l]
+        L.tp_apm_set_grid.argtypes = [p, dp, dp, dp]
+        L.tp_apm_get_grid.argtypes = [p, dp, dp, dp]
+        L.tp_apm_maps.argtypes = [p, dp, dp]
+        L.tp_apm_maps_from_kappa.argtypes = [p, dp, dp]
+        L.tp_apm_map3.argtypes = [p, i, dp]
+        L.tp_apm_extract_map3.argtypes = [p, dp, dp, dp, dp, l, i, dp]
+        L.tp_apm_extract_map3_device.argtypes = [p, p, p, p, p, l, i, p]
         L.tp_map3_batch.argtypes = [p, ip, i, dp, i, d, d, d, d, d, i, dp, dp, i64p, ip]
         L.tp_map3_jobs_device.argtypes = [p, p, p, i, d, d, d, d, d, i, p, p, p, p, p, p]
         L.tp_ctx_set_limits.argtypes = [p, i, i]

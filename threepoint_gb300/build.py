@@ -93,7 +93,7 @@ def build(force: bool = False, verbose: bool = False, extra=(), use_tuned: bool 
                 sys.stderr.write(" ".join(cmd) + "\n" + r.stdout + r.stderr)
             if r.returncode != 0:
                 raise RuntimeError("nvcc failed on " + cmd[-3])
-    link = [nvcc, *ARCH, "-shared", "-o", LIB, *objs, "-lcudart"]
+    link = [nvcc, *ARCH, "-shared", "-o", LIB, *objs, "-lcudart", "-ldl"]
     r = subprocess.run(link, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("link failed:\n" + r.stdout + r.stderr)
