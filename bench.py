@@ -547,6 +547,8 @@ def run_cov(args):
         return None
     torch.cuda.set_device(local)
     ctx = tp.Context(local)
+    if args.cov_region_cap > 0:
+        ctx.set_limits(args.cov_region_cap)
     zs, ns = nz_config()
     ctx.set_shape_noise(0.3, 10 / ARCMIN ** 2, False)
     ctx.set_cosmology(tp.cosmology(**COSMO_FID), tp.rebin_n_of_z(zs, ns, 256, 3.0))
@@ -570,6 +572,8 @@ def run_cov(args):
     n64 = min(len(pick), args.cov_fp64_pairs)
     err, t64 = {}, {}
     for name, term, geom in terms:
+        if name not in args.cov_fp64_terms.split(","):
+            continue
         t0 = time.perf_counter()
         r64 = ctx.cov_total(term, A[:n64], B[:n64], geometry=geom, precision=tp.FP64, check=False, **kw)
         t64[name] = time.perf_counter() - t0
@@ -860,6 +864,9 @@ def main():
     ap.add_argument("--cov-pairs", type=int, default=24)
     ap.add_argument("--cov-fp64-pairs", type=int, default=4)
     ap.add_argument("--cov-terms", default="T1,T2,T4", help="comma-separated subset of T1,T2,T4")
+    ap.add_argument("--cov-fp64-terms", default="T2,T4",
+                    help="terms also run in FP64 for the error (the square T1 at the cap takes minutes in FP64)")
+    ap.add_argument("--cov-region-cap", type=int, default=0, help="regions per covariance integral (0: library default)")
     ap.add_argument("--sg-cosmo", type=int, default=64)
     ap.add_argument("--sg-points", type=int, default=1 << 18, help="training triangles per cosmology")
     ap.add_argument("--sg-holdout", type=int, default=8)

@@ -416,10 +416,10 @@ static int run_engine(tp_ctx* ctx, const P& pol, int njobs, double rel_tol) {
   if (grid > njobs) grid = njobs;
   // covariance integrals (6-D square-window T1, oscillating 2-D T2) refine to
   // 10^5 regions and more: at least 2^19 regions per integral, with the grid
-  // trimmed so that the region stores stay within 24 GB of HBM
+  // trimmed so that the region stores stay within 64 GB of HBM
   const int cap = std::max(ctx->region_cap, 1 << 19);
   size_t slot = Slot<DIM, 1>::bytes(cap);
-  const size_t budget = size_t(24) << 30;
+  const size_t budget = size_t(64) << 30;
   if ((size_t)grid * slot > budget) grid = std::max(1, (int)(budget / slot));
   int st = ctx->ensure_scratch((size_t)grid * slot);
   if (st) return st;
