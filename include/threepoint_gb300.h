@@ -123,10 +123,21 @@ int tp_ctx_destroy(tp_ctx* ctx);
 void* tp_ctx_stream(tp_ctx* ctx);
 
 /* Limits of the adaptive integrals run on this context: region_cap = regions
- * per integral (default 32768; an integral that needs more stops with
- * TP_ERR_CAPACITY), max_ctas = CTAs of the persistent grid (0 = all resident).
+ * per integral (default 32768; an integral that needs more stops there, see
+ * tp_ctx_set_escalation), max_ctas = CTAs of the persistent grid (0 = all resident).
  * Device scratch = grid * region_cap * ~90 bytes (3-D integrands). */
 int tp_ctx_set_limits(tp_ctx* ctx, int region_cap, int max_ctas);
+
+/* The reference's cubature has no region cap (hcubature_v with maxEval = 0,
+ * apertureStatistics.cu:222-225, gamma.cu:110). The host-API calls
+ * tp_map3_batch and tp_gamma_batch therefore integrate the integrals that
+ * reach region_cap again, from the start, with 16x the cap (fewer CTAs, the
+ * region stores bounded to 32 GB), until they converge or reach
+ * max_region_cap (default 2^24); since the adaptive sequence is
+ * deterministic, the result is the one an uncapped run gives. Only integrals
+ * that still reach max_region_cap are reported (status bit 1,
+ * TP_ERR_CAPACITY). max_region_cap <= region_cap turns this off. */
+int tp_ctx_set_escalation(tp_ctx* ctx, int max_region_cap);
 
 /* Measured throughput of the pipes that bound the integrand kernels, whole
  * device: out[0] ex2.approx.f32 (SFU) ops/s, out[1] FP32 FMA/s, out[2] FP64 FMA/s. */

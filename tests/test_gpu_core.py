@@ -160,6 +160,7 @@ def test_region_cap_exhaustion_reports_and_recovers(nz256):
         ctx.set_limits(region_cap=63)
     ctx.set_cosmology(tp.cosmology(**COSMO1), nz256)
     ctx.set_limits(region_cap=64)
+    ctx.set_escalation(0)  # report the cap instead of integrating again
     with pytest.raises(tp.ThreepointError) as e:
         ctx.map3_batch(th, precision=tp.FP32)
     assert e.value.status == tp.TP_ERR_CAPACITY
@@ -229,3 +230,20 @@ def test_gamma_integrand_points_match_oracle(gpu_ctx, oracle_tables):
         for prec, tol in ((0, 1e-10), (1, 1e-3)):
             got = gpu_ctx.gamma_integrand_points(which, x, pts, precision=prec)
             assert np.max(np.abs(got - ref)) < tol * np.max(np.abs(ref)), (which, prec)
+
+
+def test_region_cap_escalation_reproduces_uncapped_result(nz256):
+    """With escalation on (the default), an integral that reaches a small
+    region cap is integrated again with larger caps; the value equals the one
+    of a run with a cap large enough from the start, bit for bit, since the
+    adaptive sequence is the same."""
+    import threepoint_gb300 as tp
+
+    th = [[1 * ARC, 1 * ARC, 1 * ARC], [16 * ARC, 16 * ARC, 16 * ARC]]
+    with tp.Context(0) as ctx:
+        ctx.set_cosmology(tp.cosmology(**COSMO1), nz256)
+        ref, info_ref = ctx.map3_batch(th, precision=tp.FP32, return_info=True)
+        ctx.set_limits(region_cap=64)
+        got, info = ctx.map3_batch(th, precision=tp.FP32, return_info=True)
+    assert np.all(info["status"] == 0)
+    assert np.array_equal(got, ref) and np.array_equal(info["neval"], info_ref["neval"])

@@ -69,3 +69,25 @@ def test_gamma_rejects_invalid_triangles(gpu_ctx):
         gpu_ctx.gamma_batch([(1e-3, 1e-3, 5e-3)])
     with pytest.raises(tp.ThreepointError):
         gpu_ctx.gamma_batch([(1e-3, 0.0, 1e-3)])
+
+
+def test_gamma_region_cap_escalation_matches_oracle(nz256, oracle_tables):
+    """A flat small triangle of the calculateGamma grid (r = 0.178', u = 0.05,
+    v = 0.7: about 15600 regions for Gamma^0) on a context whose region cap is
+    1024: the integral reaches the cap, is integrated again with larger caps
+    until it converges, as the reference's unbounded hcubature_v does, and
+    matches the oracle."""
+    import threepoint_gb300 as tp
+    from conftest import COSMO1
+
+    O.set_threads(0)
+    r2 = 0.178 * ARC
+    r3 = 0.05 * r2
+    x = (0.7 * r3 + r2, r2, r3)
+    ref = oracle_tables.gamma(0, *x)[0]
+    with tp.Context(0) as ctx:
+        ctx.set_limits(region_cap=1024)
+        ctx.set_cosmology(tp.cosmology(**COSMO1), nz256)
+        got = ctx.gamma_batch([x], comp_mask=1, precision=0)[0, 0]
+        assert ctx.last_gamma_status[0] == 0
+    assert abs(got - ref) <= 1e-6 * abs(ref), (got, ref)

@@ -172,6 +172,7 @@ def lib():
         L.tp_map3_batch.argtypes = [p, ip, i, dp, i, d, d, d, d, d, i, dp, dp, i64p, ip]
         L.tp_map3_jobs_device.argtypes = [p, p, p, i, d, d, d, d, d, i, p, p, p, p, p, p]
         L.tp_ctx_set_limits.argtypes = [p, i, i]
+        L.tp_ctx_set_escalation.argtypes = [p, i]
         L.tp_map3_jobs_noalloc.argtypes = [p, p, p, i, d, d, d, d, d, i, p, p, p]
         L.tp_ctx_stream.restype = p
         L.tp_ctx_stream.argtypes = [p]
@@ -284,6 +285,11 @@ class Context:
     def set_limits(self, region_cap=32768, max_ctas=0):
         """Regions per adaptive integral and CTAs of the persistent grid."""
         _check(self._h, lib().tp_ctx_set_limits(self._h, region_cap, max_ctas))
+
+    def set_escalation(self, max_region_cap=1 << 24):
+        """Integrals of map3_batch / gamma_batch that reach the region cap are
+        integrated again with larger caps up to max_region_cap (0: off)."""
+        _check(self._h, lib().tp_ctx_set_escalation(self._h, max_region_cap))
 
     def close(self):
         if self._h:

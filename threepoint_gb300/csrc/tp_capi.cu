@@ -19,6 +19,7 @@
 #include "tp_kernels.cuh"
 #include "tp_tables.cuh"
 #include "tp_capi_internal.h"
+#include "tp_cubature.cuh"
 
 using namespace tp;
 
@@ -565,11 +566,18 @@ extern "C" int tp_bkappa_nodes(tp_ctx* ctx, int cosmo_index, const double* ell, 
 // <Map^3>
 // ---------------------------------------------------------------------------
 static const int MAP3_MAX_SWEEPS = 2000;
+static const size_t MAP3_ESCALATE_BYTES = size_t(32) << 30;
 
 extern "C" int tp_ctx_set_limits(tp_ctx* ctx, int region_cap, int max_ctas) {
   if (!ctx || region_cap < 64 || max_ctas < 0) return TP_ERR_ARG;
   ctx->region_cap = region_cap;
   ctx->max_ctas = max_ctas;
+  return TP_OK;
+}
+
+extern "C" int tp_ctx_set_escalation(tp_ctx* ctx, int max_region_cap) {
+  if (!ctx || max_region_cap < 0) return TP_ERR_ARG;
+  ctx->escalate_cap = max_region_cap;
   return TP_OK;
 }
 
@@ -687,6 +695,59 @@ extern "C" int tp_map3_batch(tp_ctx* ctx, const int* cosmo_index, int n_cosmo, c
   if (e == cudaSuccess) e = cudaMemcpyAsync(hst.data(), b + o_st, sizeof(int) * nj, cudaMemcpyDeviceToHost, s);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);
   if (e != cudaSuccess) return tp_cuda(ctx, e, "map3");
+  // integrals that reached the region cap: integrated again, from the start,
+  // with 16x the cap on as many CTAs as fit MAP3_ESCALATE_BYTES of region
+  // stores, up to ctx->escalate_cap (the reference's hcubature_v has no cap;
+  // the adaptive sequence is deterministic, so the larger cap continues where
+  // the smaller one stopped)
+  for (int cap = ctx->region_cap; cap < ctx->escalate_cap;) {
+    std::vector<int> again;
+    for (int j = 0; j < nj; ++j)
+      if (hst[j] & 1) again.push_back(j);
+    if (again.empty()) break;
+    cap = (int)std::min<long>((long)cap * 16, ctx->escalate_cap);
+    const int na = (int)again.size();
+    std::vector<int> ac(na);
+    std::vector<double> at(3 * (size_t)na);
+    for (int k = 0; k < na; ++k) {
+      ac[k] = jc[again[k]];
+      for (int q = 0; q < 3; ++q) at[3 * (size_t)k + q] = jt[3 * (size_t)again[k] + q];
+    }
+    e = cudaMemcpyAsync(b + o_th, at.data(), sizeof(double) * 3 * na, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(b + o_c, ac.data(), sizeof(int) * na, cudaMemcpyHostToDevice, s);
+    if (e != cudaSuccess) return tp_cuda(ctx, e, "map3 escalation upload");
+    const int saved_cap = ctx->region_cap, saved_ctas = ctx->max_ctas;
+    ctx->region_cap = cap;
+    ctx->max_ctas = (int)std::max<size_t>(1, MAP3_ESCALATE_BYTES / Slot<3, 1>::bytes(cap));
+    if (saved_ctas > 0) ctx->max_ctas = std::min(ctx->max_ctas, saved_ctas);
+    st = tp_map3_jobs_device(ctx, (int*)(b + o_c), (double*)(b + o_th), na, phi_min, phi_max, l_min, l_max, rel_tol,
+                             precision, (double*)(b + o_out), (double*)(b + o_err), (int64_t*)(b + o_nev), nullptr,
+                             (int*)(b + o_st), nullptr);
+    ctx->region_cap = saved_cap;
+    ctx->max_ctas = saved_ctas;
+    if (st) return st;
+    std::vector<double> ao(na), ae(na);
+    std::vector<int64_t> an(na);
+    std::vector<int> as(na);
+    e = cudaMemcpyAsync(ao.data(), b + o_out, sizeof(double) * na, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(ae.data(), b + o_err, sizeof(double) * na, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(an.data(), b + o_nev, sizeof(int64_t) * na, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(as.data(), b + o_st, sizeof(int) * na, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return tp_cuda(ctx, e, "map3 escalation");
+    for (int k = 0; k < na; ++k) {
+      const int j = again[k];
+      out[j] = ao[k];
+      if (err) err[j] = ae[k];
+      hnev[j] = an[k];
+      hst[j] = as[k];
+    }
+  }
+  if (ctx->scratch_bytes > (size_t(4) << 30)) {  // region stores grown by the escalation are released
+    cudaFree(ctx->d_scratch);
+    ctx->d_scratch = nullptr;
+    ctx->scratch_bytes = 0;
+  }
   if (neval) memcpy(neval, hnev.data(), sizeof(int64_t) * nj);
   for (int t = 0; t < n_trip; ++t) {
     double m = 0;

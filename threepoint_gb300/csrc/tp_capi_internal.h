@@ -25,6 +25,10 @@ struct tp_ctx {
   std::string err;
   int max_ctas = 0;        // 0 = all resident CTAs
   int region_cap = 32768;  // regions per adaptive integral
+  // integrals of the host-API calls that reach region_cap are integrated
+  // again with 16x the cap, up to this many regions (the reference's
+  // hcubature_v has no cap); <= region_cap turns this off
+  int escalate_cap = 1 << 24;
 
   // cosmologies and their device tables
   int n_cosmo = 0;

@@ -22,6 +22,7 @@
 #define TP_GAMMA_MINB 2
 #endif
 
+#include <algorithm>
 #include <cmath>
 #include <complex>
 #include <string>
@@ -375,7 +376,7 @@ constexpr int GAMMA_NT = 256;
 
 template <typename R>
 static int run_gamma(tp_ctx* ctx, int cosmo, const double* d_x, const int* d_comp, const int* d_tri, int njobs,
-                     double rel_tol, double* d_out, int* d_status) {
+                     double rel_tol, double* d_out, int* d_status, int cap, int max_ctas) {
   size_t smem = gamma_smem_bytes<R>();
   cudaError_t e =
       cudaFuncSetAttribute(k_gamma<R, GAMMA_NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -385,9 +386,9 @@ static int run_gamma(tp_ctx* ctx, int cosmo, const double* d_x, const int* d_com
   e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_gamma<R, GAMMA_NT>, GAMMA_NT, smem);
   if (e != cudaSuccess || per_sm < 1) return tp_cuda(ctx, e == cudaSuccess ? cudaErrorInvalidConfiguration : e, "gamma occupancy");
   int grid = sms * per_sm;
-  if (ctx->max_ctas > 0 && grid > ctx->max_ctas) grid = ctx->max_ctas;
+  if (max_ctas > 0 && grid > max_ctas) grid = max_ctas;
   if (grid > njobs) grid = njobs;
-  size_t slot = Slot<3, 2>::bytes(ctx->region_cap);
+  size_t slot = Slot<3, 2>::bytes(cap);
   int st = ctx->ensure_scratch((size_t)grid * slot);
   if (st) return st;
   GammaPolicy<R> pol;
@@ -400,7 +401,7 @@ static int run_gamma(tp_ctx* ctx, int cosmo, const double* d_x, const int* d_com
   pol.cosmo = cosmo;
   pol.out = d_out;
   pol.status = d_status;
-  EngineCfg cfg{0.0, rel_tol, TP_NORM_L1, ctx->region_cap, 2000};
+  EngineCfg cfg{0.0, rel_tol, TP_NORM_L1, cap, 2000};
   e = cudaMemsetAsync(ctx->d_counter, 0, sizeof(int), ctx->stream);
   if (e == cudaSuccess) {
     k_gamma<R, GAMMA_NT><<<grid, GAMMA_NT, smem, ctx->stream>>>(pol, njobs, ctx->d_counter, cfg, ctx->d_scratch, slot);
@@ -481,6 +482,56 @@ extern "C" int tp_gamma_integrand_points(tp_ctx* ctx, int cosmo_index, const dou
   return tp_cuda(ctx, e, "gamma points");
 }
 
+// One pass of the Gamma integrals of n triangles (components of comp_mask)
+// at region cap `cap` on at most max_ctas CTAs (0: all resident); out is
+// [n][4] complex as 8 doubles, status_out[n] the OR of the triangle's
+// components' engine status (bit 1: region cap reached).
+static int gamma_pass(tp_ctx* ctx, int cosmo_index, const double* x, int n, int comp_mask, double rel_tol,
+                      int precision, int cap, int max_ctas, double* out, int* status_out) {
+  std::vector<int> comp, tri;
+  for (int t = 0; t < n; ++t)
+    for (int c = 0; c < 4; ++c)
+      if (comp_mask & (1 << c)) {
+        comp.push_back(c);
+        tri.push_back(t);
+      }
+  const int nj = (int)comp.size();
+  size_t o_x = 0, o_c = (sizeof(double) * 3 * n + 255) & ~size_t(255);
+  size_t o_t = o_c + ((sizeof(int) * nj + 255) & ~size_t(255));
+  size_t o_o = o_t + ((sizeof(int) * nj + 255) & ~size_t(255));
+  size_t o_s = o_o + ((sizeof(double) * 8 * n + 255) & ~size_t(255));
+  int st = ctx->ensure_io(o_s + sizeof(int) * n + 256);
+  if (st) return st;
+  char* b = ctx->d_io;
+  cudaStream_t s = ctx->stream;
+  cudaError_t e = cudaMemcpyAsync(b + o_x, x, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(b + o_c, comp.data(), sizeof(int) * nj, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(b + o_t, tri.data(), sizeof(int) * nj, cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(b + o_o, 0, sizeof(double) * 8 * n, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(b + o_s, 0, sizeof(int) * n, s);
+  if (e != cudaSuccess) return tp_cuda(ctx, e, "gamma upload");
+  st = precision == TP_FP64
+           ? run_gamma<double>(ctx, cosmo_index, (double*)(b + o_x), (int*)(b + o_c), (int*)(b + o_t), nj, rel_tol,
+                               (double*)(b + o_o), (int*)(b + o_s), cap, max_ctas)
+           : run_gamma<float>(ctx, cosmo_index, (double*)(b + o_x), (int*)(b + o_c), (int*)(b + o_t), nj, rel_tol,
+                              (double*)(b + o_o), (int*)(b + o_s), cap, max_ctas);
+  if (st) return st;
+  e = cudaMemcpyAsync(out, b + o_o, sizeof(double) * 8 * n, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(status_out, b + o_s, sizeof(int) * n, cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  return tp_cuda(ctx, e, "gamma");
+}
+
+// The reference integrates Gamma with an unbounded hcubature_v (maxEval = 0,
+// gamma.cu:110). Triangles whose integrals reach the context's region cap are
+// integrated again, from the start, with a cap 16 times larger on as many
+// CTAs as fit GAMMA_ESCALATE_BYTES of region stores, up to the context's
+// escalation cap (at most GAMMA_CAP_MAX regions per integral); the adaptive
+// sequence is deterministic, so the larger cap continues exactly where the
+// smaller one stopped. Only what still reaches the last cap is reported.
+constexpr int GAMMA_CAP_MAX = 1 << 24;
+constexpr size_t GAMMA_ESCALATE_BYTES = size_t(32) << 30;
+
 extern "C" int tp_gamma_batch(tp_ctx* ctx, int cosmo_index, const double* x, int n, int comp_mask, double rel_tol,
                               int precision, double* out, int* status_out) {
   TpRange nvtx_range("tp_gamma_batch: Gamma");
@@ -498,39 +549,38 @@ extern "C" int tp_gamma_batch(tp_ctx* ctx, int cosmo_index, const double* x, int
   cudaSetDevice(ctx->device);
   cudaError_t e = gamma_upload_constants();
   if (e != cudaSuccess) return tp_cuda(ctx, e, "ogata constants");
-  std::vector<int> comp, tri;
-  for (int t = 0; t < n; ++t)
-    for (int c = 0; c < 4; ++c)
-      if (comp_mask & (1 << c)) {
-        comp.push_back(c);
-        tri.push_back(t);
-      }
-  const int nj = (int)comp.size();
-  size_t o_x = 0, o_c = (sizeof(double) * 3 * n + 255) & ~size_t(255);
-  size_t o_t = o_c + ((sizeof(int) * nj + 255) & ~size_t(255));
-  size_t o_o = o_t + ((sizeof(int) * nj + 255) & ~size_t(255));
-  size_t o_s = o_o + ((sizeof(double) * 8 * n + 255) & ~size_t(255));
-  int st = ctx->ensure_io(o_s + sizeof(int) * n + 256);
-  if (st) return st;
-  char* b = ctx->d_io;
-  cudaStream_t s = ctx->stream;
-  e = cudaMemcpyAsync(b + o_x, x, sizeof(double) * 3 * n, cudaMemcpyHostToDevice, s);
-  if (e == cudaSuccess) e = cudaMemcpyAsync(b + o_c, comp.data(), sizeof(int) * nj, cudaMemcpyHostToDevice, s);
-  if (e == cudaSuccess) e = cudaMemcpyAsync(b + o_t, tri.data(), sizeof(int) * nj, cudaMemcpyHostToDevice, s);
-  if (e == cudaSuccess) e = cudaMemsetAsync(b + o_o, 0, sizeof(double) * 8 * n, s);
-  if (e == cudaSuccess) e = cudaMemsetAsync(b + o_s, 0, sizeof(int) * n, s);
-  if (e != cudaSuccess) return tp_cuda(ctx, e, "gamma upload");
-  st = precision == TP_FP64
-           ? run_gamma<double>(ctx, cosmo_index, (double*)(b + o_x), (int*)(b + o_c), (int*)(b + o_t), nj, rel_tol,
-                               (double*)(b + o_o), (int*)(b + o_s))
-           : run_gamma<float>(ctx, cosmo_index, (double*)(b + o_x), (int*)(b + o_c), (int*)(b + o_t), nj, rel_tol,
-                              (double*)(b + o_o), (int*)(b + o_s));
-  if (st) return st;
   std::vector<int> hst(n);
-  e = cudaMemcpyAsync(out, b + o_o, sizeof(double) * 8 * n, cudaMemcpyDeviceToHost, s);
-  if (e == cudaSuccess) e = cudaMemcpyAsync(hst.data(), b + o_s, sizeof(int) * n, cudaMemcpyDeviceToHost, s);
-  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-  if (e != cudaSuccess) return tp_cuda(ctx, e, "gamma");
+  int st = gamma_pass(ctx, cosmo_index, x, n, comp_mask, rel_tol, precision, ctx->region_cap, ctx->max_ctas, out,
+                      hst.data());
+  if (st) return st;
+  for (int cap = ctx->region_cap; cap < std::min(GAMMA_CAP_MAX, ctx->escalate_cap);) {
+    std::vector<int> again;
+    for (int t = 0; t < n; ++t)
+      if (hst[t] & 1) again.push_back(t);
+    if (again.empty()) break;
+    cap = (int)std::min<long>((long)cap * 16, std::min(GAMMA_CAP_MAX, ctx->escalate_cap));
+    const int nj = (int)again.size() * __builtin_popcount((unsigned)comp_mask);
+    int ctas = (int)std::max<size_t>(1, GAMMA_ESCALATE_BYTES / Slot<3, 2>::bytes(cap));
+    if (ctx->max_ctas > 0) ctas = std::min(ctas, ctx->max_ctas);
+    ctas = std::min(ctas, nj);
+    std::vector<double> xs(3 * again.size()), os(8 * again.size());
+    std::vector<int> ss(again.size());
+    for (size_t k = 0; k < again.size(); ++k)
+      for (int q = 0; q < 3; ++q) xs[3 * k + q] = x[3 * again[k] + q];
+    st = gamma_pass(ctx, cosmo_index, xs.data(), (int)again.size(), comp_mask, rel_tol, precision, cap, ctas,
+                    os.data(), ss.data());
+    if (st) return st;
+    for (size_t k = 0; k < again.size(); ++k) {
+      for (int q = 0; q < 8; ++q) out[8 * again[k] + q] = os[8 * k + q];
+      hst[again[k]] = ss[k];
+    }
+  }
+  // region stores grown by the escalation are released again
+  if (ctx->scratch_bytes > (size_t(4) << 30)) {
+    cudaFree(ctx->d_scratch);
+    ctx->d_scratch = nullptr;
+    ctx->scratch_bytes = 0;
+  }
   int bad = 0;
   for (int t = 0; t < n; ++t) {
     if (status_out) status_out[t] = hst[t];
