@@ -41,7 +41,7 @@ N_LHS = 4096
 # (4 LHS cosmologies x 220 triplets: 65.9 + 221.5 MB); the region-store
 # traffic grows with the number of integrals
 TRAFFIC_PER_INTEGRAL = (70.184192e6 + 225.050112e6) / 880
-SFU_PER_NODE = 19  # SFU ops (ex2/rcp.approx) per line-of-sight node of the FP32 BiHalofit evaluation (NF_* rows, merged reciprocals, kk P table)
+SFU_PER_NODE = 22  # SFU ops (ex2/rcp.approx) per line-of-sight node of the FP32 BiHalofit evaluation (NF_* rows, merged reciprocals)
 NNODE = 96
 
 

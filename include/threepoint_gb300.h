@@ -273,6 +273,8 @@ int tp_gamma_batch(tp_ctx* ctx, int cosmo_index, const double* x, int n, int com
 typedef struct tp_apm tp_apm;
 int tp_apm_create(tp_ctx* ctx, int npix, double fieldsize, const double* thetas, int n_theta, int polynomial,
                   tp_apm** out);
+/* A tp_apm's calls need its context; destroying it does not (it may come
+ * after tp_ctx_destroy). */
 int tp_apm_destroy(tp_apm* apm);
 /* FFT grid side F >= 2 npix - 1 of the zero-padded convolutions */
 int tp_apm_fft_size(const tp_apm* apm);

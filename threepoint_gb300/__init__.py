@@ -286,12 +286,26 @@ class Context:
         """Regions per adaptive integral and CTAs of the persistent grid."""
         _check(self._h, lib().tp_ctx_set_limits(self._h, region_cap, max_ctas))
 
+    def _adopt(self, child):
+        """Objects holding device state made with this context (aperture-mass
+        plans) are closed before the context."""
+        import weakref
+
+        if not hasattr(self, "_children"):
+            self._children = []
+        self._children.append(weakref.ref(child))
+
     def set_escalation(self, max_region_cap=1 << 24):
         """Integrals of map3_batch / gamma_batch that reach the region cap are
         integrated again with larger caps up to max_region_cap (0: off)."""
         _check(self._h, lib().tp_ctx_set_escalation(self._h, max_region_cap))
 
     def close(self):
+        for r in getattr(self, "_children", []):
+            c = r()
+            if c is not None:
+                c.close()
+        self._children = []
         if self._h:
             lib().tp_ctx_destroy(self._h)
             self._h = C.c_void_p(0)

@@ -45,6 +45,7 @@ class _Plan:
         th = _arr(self.thetas)
         _check(ctx._h, lib().tp_apm_create(ctx._h, self.npix, self.fieldsize, _dp(th), len(th), int(polynomial),
                                            C.byref(self._h)))
+        ctx._adopt(self)
 
     def close(self):
         if self._h:
@@ -136,6 +137,8 @@ class aperture_mass_computer:
 
     def change_theta_ap(self, theta_ap):
         self.theta_ap = float(theta_ap)
+        if self._plan is not None:
+            self._plan.close()
         self._plan = None
 
     def _p(self):

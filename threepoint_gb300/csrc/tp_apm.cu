@@ -284,7 +284,8 @@ unsigned blocks_for(long n, int bs) { return (unsigned)((n + bs - 1) / bs); }
 
 // ---------------------------------------------------------------------------
 struct tp_apm {
-  tp_ctx* ctx = nullptr;
+  tp_ctx* ctx = nullptr;  // must outlive the tp_apm's calls (not its destruction)
+  int device = 0;
   int npix = 0, F = 0, n_theta = 0, polynomial = 0;
   double fieldsize = 0;
   std::vector<double> thetas;
@@ -442,6 +443,7 @@ extern "C" int tp_apm_create(tp_ctx* ctx, int npix, double fieldsize, const doub
   cudaSetDevice(ctx->device);
   tp_apm* a = new tp_apm();
   a->ctx = ctx;
+  a->device = ctx->device;
   a->npix = npix;
   a->fieldsize = fieldsize;
   a->n_theta = n_theta;
@@ -520,7 +522,8 @@ extern "C" int tp_apm_create(tp_ctx* ctx, int npix, double fieldsize, const doub
 
 extern "C" int tp_apm_destroy(tp_apm* a) {
   if (!a) return TP_OK;
-  cudaSetDevice(a->ctx->device);
+  // only the device is used here: the context may already be gone
+  cudaSetDevice(a->device);
   const CufftApi& api = cufft();
   if (a->have_fwd) api.destroy(a->fwd);
   if (a->have_inv) api.destroy(a->inv);

@@ -54,7 +54,7 @@ struct CosmoK {
   // clamping the coordinate at every node)
   R lgp_lo, lgp_hi;
   const double* pk;   // 256 values (FP64, read through the cache)
-  const float* plt;   // kk P_lin cubic segments (PLT_N float4) for the FP32 path, or null
+  const float* plt;   // log2 P_lin cubic segments (PLT_N float4) for the FP32 path, or null
 };
 
 template <typename R>
@@ -104,7 +104,7 @@ __device__ __forceinline__ R plin(const CosmoK<R>& K, R kk, R l2kk) {
       int i = (int)t;
       float f = t - (float)i;
       const float4 q = reinterpret_cast<const float4*>(K.plt)[i];
-      return (q.x + f * (q.y + f * (q.z + f * q.w))) * M::rcp(kk);  // D / kk
+      return M::ex2(q.x + f * (q.y + f * (q.z + f * q.w)));
     }
   }
   R x = kk * K.sh043;
@@ -271,10 +271,9 @@ __device__ __forceinline__ R bispec_node(const R* __restrict__ nc, int j, const 
 
 // ---------------------------------------------------------------------------
 // FP32 point path of <Map^3> and b_kappa: NF_* node rows (tp_internal.cuh).
-// Per triangle it keeps ell_i^2 and 1/ell_i besides the Tri fields; the
-// record is 18 words.
+// Per triangle it keeps ell_i^2 besides the Tri fields; the record is 15 words.
 struct TriF {
-  float l[3], lg[3], l2[3], il[3];
+  float l[3], lg[3], l2[3];
   float log2r1, r2sq, pr2;
   float f2t[3];
 };
@@ -285,7 +284,6 @@ __device__ __forceinline__ void trif_from_tri(const Tri<float>& T, TriF& F) {
     F.l[i] = T.l[i];
     F.lg[i] = T.lg[i];
     F.l2[i] = T.l[i] * T.l[i];
-    F.il[i] = Mth<float>::rcp(T.l[i]);
     F.f2t[i] = T.f2t[i];
   }
   F.log2r1 = T.log2r1;
@@ -293,33 +291,22 @@ __device__ __forceinline__ void trif_from_tri(const Tri<float>& T, TriF& F) {
   F.pr2 = T.pr2;
 }
 
-// D(kk) = kk P_lin(kk) at kk = ell h / f_K from the node's row and the cubic
-// table (table coordinate lg * (N-1)/(HI-LO) + NF_TOFF; the integer part by a
-// round-down add of 1.5 * 2^23, no float/int conversions)
-__device__ __forceinline__ float plin_table_d(const CosmoK<float>& K, const float* __restrict__ c, float lg) {
-  constexpr float INV = (float)((PLT_N - 1) / (PLT_HI - PLT_LO));
-  float t = fmaf(lg, INV, c[NF_TOFF]);
-  t = fminf(fmaxf(t, 0.f), (float)(PLT_N - 1) - 1e-3f);
-  const float tm = __fadd_rd(t, 12582912.f);  // 1.5 * 2^23 + floor(t)
-  const int i = __float_as_int(tm) - 0x4B400000;
-  const float f = t - (tm - 12582912.f);
-  const float4 q = reinterpret_cast<const float4*>(K.plt)[i];
-  return fmaf(f, fmaf(f, fmaf(f, q.w, q.z), q.y), q.x);
-}
-
-// P_lin(ell h / f_K) from the node's row: the cubic table when present, else plin()
+// P_lin(ell h / f_K) from the node's row: the cubic log2 P table when present
+// (table coordinate lg * (N-1)/(HI-LO) + NF_TOFF; the integer part by a
+// round-down add of 1.5 * 2^23, no float/int conversions), else plin().
 __device__ __forceinline__ float plin_fast(const CosmoK<float>& K, const float* __restrict__ c, float l, float lg) {
-  if (K.plt) return plin_table_d(K, c, lg) * Mth<float>::rcp(l * c[NF_HF]);
+  typedef Mth<float> M;
+  if (K.plt) {
+    constexpr float INV = (float)((PLT_N - 1) / (PLT_HI - PLT_LO));
+    float t = fmaf(lg, INV, c[NF_TOFF]);
+    t = fminf(fmaxf(t, 0.f), (float)(PLT_N - 1) - 1e-3f);
+    const float tm = __fadd_rd(t, 12582912.f);  // 1.5 * 2^23 + floor(t)
+    const int i = __float_as_int(tm) - 0x4B400000;
+    const float f = t - (tm - 12582912.f);
+    const float4 q = reinterpret_cast<const float4*>(K.plt)[i];
+    return M::ex2(fmaf(f, fmaf(f, fmaf(f, q.w, q.z), q.y), q.x));
+  }
   return plin<float>(K, l * c[NF_HF], lg + c[NF_L2HF]);
-}
-
-// P_lin(ell h / f_K) h / f_K, the form the 3-halo term reads (its NF_D1SQ*
-// coefficients carry f_K / h): D / ell from the table (il = 1 / ell), no
-// special-function operation
-__device__ __forceinline__ float plin_scaled(const CosmoK<float>& K, const float* __restrict__ c, float l, float il,
-                                            float lg) {
-  if (K.plt) return plin_table_d(K, c, lg) * il;
-  return plin<float>(K, l * c[NF_HF], lg + c[NF_L2HF]) * c[NF_HF];
 }
 
 // plin<float> kept out of line: the tabulated-P(k) and Eisenstein & Hu
@@ -381,7 +368,7 @@ __device__ __forceinline__ float2 p2rcp(float2 a) { return make_float2(Mth<float
 
 // The triangle of TriF with every field duplicated into both lanes of a pair.
 struct TriF2 {
-  float2 l[3], lg[3], l2[3], il[3];
+  float2 l[3], lg[3], l2[3];
   float2 log2r1, r2sq, pr2;
   float2 f2t[3];
   float2 lgp[3];  // log2 ell_i clamped into [lgp_lo, lgp_hi] (P(k) table lookups only)
@@ -394,7 +381,6 @@ __device__ __forceinline__ void trif2_from(const TriF& T, TriF2& D, float lgp_lo
     D.l[i] = p2dup(T.l[i]);
     D.lg[i] = p2dup(T.lg[i]);
     D.l2[i] = p2dup(T.l2[i]);
-    D.il[i] = p2dup(T.il[i]);
     D.f2t[i] = p2dup(T.f2t[i]);
   }
   D.log2r1 = p2dup(T.log2r1);
@@ -511,13 +497,13 @@ __device__ __forceinline__ float2 bispec_pair(const float2* __restrict__ c, cons
         for (int h = 0; h < 2; ++h) {
           const float f = tf[h];
           const float4 q = reinterpret_cast<const float4*>(K.plt)[ixs[h]];
-          r[h] = fmaf(f, fmaf(f, fmaf(f, q.w, q.z), q.y), q.x);  // D = kk P
+          r[h] = M::ex2(fmaf(f, fmaf(f, fmaf(f, q.w, q.z), q.y), q.x));
         }
-        pl = p2mul(make_float2(r[0], r[1]), v2(T.il[i]));  // P h / f_K = D / ell
+        pl = make_float2(r[0], r[1]);
       } else {
         const float2 hf = c[NF_HF], l2hf = c[NF_L2HF];
-        pl.x = plin_outline(&K, v2(T.l[i]).x * hf.x, v2(T.lg[i]).x + l2hf.x) * hf.x;
-        pl.y = plin_outline(&K, v2(T.l[i]).y * hf.y, v2(T.lg[i]).y + l2hf.y) * hf.y;
+        pl.x = plin_outline(&K, v2(T.l[i]).x * hf.x, v2(T.lg[i]).x + l2hf.x);
+        pl.y = plin_outline(&K, v2(T.l[i]).y * hf.y, v2(T.lg[i]).y + l2hf.y);
       }
     }
     const float2 x = p2mul(c[NF_PNS], v2(T.l[i]));
@@ -576,7 +562,7 @@ __device__ __forceinline__ float bispec_fast_row(const float* c, const TriF& T, 
     for (int i = 0; i < 3; ++i) {
       const float num = fmaf(c[NF_D1SQFNS2], T.l2[i], c[NF_D1SQ]);
       const float den = fmaf(c[NF_HNS2], T.l2[i], fmaf(c[NF_GNS], T.l[i], 1.f));
-      const float a = num * M::rcp(den) * plin_scaled(K, c, T.l[i], T.il[i], T.lg[i]);
+      const float a = num * M::rcp(den) * plin_fast(K, c, T.l[i], T.lg[i]);
       const float x = c[NF_PNS] * T.l[i];
       const float x3 = x * x * x;
       const float mq = M::ex2(fmaf(c[NF_MUN], lq[i], c[NF_L2MN])) + M::ex2(fmaf(c[NF_NUN], lq[i], c[NF_L2NN]));
@@ -619,9 +605,8 @@ __device__ __forceinline__ void nf_from_nc(const float* zc, float* nf) {
   nf[NF_ALA] = zc[NC_ALA];
   nf[NF_ALD] = zc[NC_ALD];
   nf[NF_BETAB] = zc[NC_BETAB];
-  const float ihf = M::rcp(zc[NC_HF]);  // the 3-halo term reads P h / f_K
-  nf[NF_D1SQ] = zc[NC_D1SQ] * ihf;
-  nf[NF_D1SQFNS2] = zc[NC_D1SQ] * zc[NC_FN] * s * s * ihf;
+  nf[NF_D1SQ] = zc[NC_D1SQ];
+  nf[NF_D1SQFNS2] = zc[NC_D1SQ] * zc[NC_FN] * s * s;
   nf[NF_GNS] = zc[NC_GN] * s;
   nf[NF_HNS2] = zc[NC_HN] * s * s;
   nf[NF_L2MN] = M::lg2(zc[NC_MN]);
@@ -637,16 +622,14 @@ __device__ __forceinline__ void nf_from_nc(const float* zc, float* nf) {
   for (int k = NF_COUNT; k < NCP; ++k) nf[k] = 0.f;
 }
 
-// the triangle scaled by sc (log2 l2sc, isc = 1/sc): ell_i -> ell_i sc; shape
-// factors unchanged
-__device__ __forceinline__ TriF trif_scaled(const TriF& T, float sc, float l2sc, float isc) {
+// the triangle scaled by sc (log2 l2sc): ell_i -> ell_i sc; shape factors unchanged
+__device__ __forceinline__ TriF trif_scaled(const TriF& T, float sc, float l2sc) {
   TriF S = T;
   const float sc2 = sc * sc;
 #pragma unroll
   for (int i = 0; i < 3; ++i) {
     S.l[i] = T.l[i] * sc;
     S.l2[i] = T.l2[i] * sc2;
-    S.il[i] = T.il[i] * isc;
     S.lg[i] = T.lg[i] + l2sc;
   }
   return S;

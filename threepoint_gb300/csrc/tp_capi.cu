@@ -348,6 +348,7 @@ extern "C" int tp_ctx_create(int device, tp_ctx** out) {
   if (device < 0 || device >= ndev) return TP_ERR_ARG;
   tp_ctx* c = new tp_ctx();
   c->device = device;
+  cudaGetLastError();  // a stale error left by other code in the process is not this context's
   if (cudaSetDevice(device) != cudaSuccess) {
     delete c;
     return TP_ERR_CUDA;

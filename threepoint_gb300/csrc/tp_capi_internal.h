@@ -48,7 +48,7 @@ struct tp_ctx {
   double* d_wscale32 = nullptr;
   void* d_ck64 = nullptr;
   void* d_ck32 = nullptr;
-  float4* d_plt = nullptr;  // [n_cosmo][PLT_N] cubic segments of kk P_lin(kk)
+  float4* d_plt = nullptr;  // [n_cosmo][PLT_N] log2 P_lin cubic segments
   double* d_ehg = nullptr;  // [n_cosmo][EHG_N] 2 ln T(k) of the sigma(R) integrand
 
   // shape noise of P(ell)

@@ -117,7 +117,7 @@ struct GammaPolicy {
   static constexpr int KPG = 4;
   static constexpr int CH = 4;    // regions per chunk (records are large)
   // FP64: the per-point NC_* coefficients (bispec_eval); FP32: the folded
-  // NF_* row (bispec_fast_row), an odd number of words (61) per record
+  // NF_* row (bispec_fast_row), an odd number of words (57) per record
   struct RecD {
     double zc[NC_COUNT];
     Tri<double> tri;  // unit-scale triangle (cos psi, sin psi, ell3/psi_k)
@@ -133,7 +133,6 @@ struct GammaPolicy {
     float cre[3], cim[3];
     float bmin;
     int live;
-    float pad;  // odd word count: consecutive records start in different banks
   };
   typedef typename std::conditional<sizeof(R) == 4, RecF, RecD>::type Rec;
   static constexpr int REC = (int)sizeof(Rec);
@@ -277,7 +276,7 @@ struct GammaPolicy {
         for (int j = 0; j < 3; ++j) {
           const float sc = psik * r.invA[j];
           if (r.bmin * sc <= 1.0e-10f) continue;  // integrand_bkappa: ell <= 1e-10 -> 0
-          const TriF T = trif_scaled(r.tri, sc, l2psik - r.l2A[j], Mth<float>::rcp(sc));
+          const TriF T = trif_scaled(r.tri, sc, l2psik - r.l2A[j]);
           float v = W * bispec_fast_row(c, T, K);
           if (v != v) v = 0.f;  // NaN -> 0 (bispectrum.cu:327-331)
           v *= prodk;

@@ -18,13 +18,9 @@ constexpr double PI = 3.14159265358979323846;
 constexpr double LOG2_10 = 3.32192809488736234787;
 constexpr double LN2 = 0.69314718055994530942;
 // FP32 integrands read the Eisenstein & Hu linear P(k) from a per-cosmology
-// table of D(kk) = kk P(kk), kk = k h, on a uniform log2(kk) grid, interpolated
-// by Catmull-Rom cubics (relative error <= 5e-6 over the grid, checked on the
-// box corners). kk P has log-log slopes between about -2 and +2 where P itself
-// runs from k^n_s to k^-3, so a cubic in D is accurate without the
-// exponential a log2 P table needs: P = D / kk, and at a line-of-sight node
-// with kk = ell h/f_K the 3-halo term takes P h/f_K = D / ell, where 1/ell is
-// kept per cubature point. FP64 integrands evaluate the fit itself.
+// table of log2 P on a uniform log2(k h) grid, interpolated by Catmull-Rom
+// cubics (relative error ~1e-6 over the grid); FP64 integrands evaluate the
+// fit itself.
 constexpr int PLT_N = 1024;  // grid points; the table stores per interval (y0, c1, c2, c3) of the cubic
 constexpr double PLT_LO = -24.0, PLT_HI = 24.0;
 // 2 ln T(k) of the Eisenstein & Hu no-wiggle transfer function, the part of
@@ -103,8 +99,8 @@ enum FastCoef {
   NF_L2BN,      // log2 b_n
   NF_CNS,       // c_n s
   NF_ALA, NF_ALD, NF_BETAB,
-  NF_D1SQ,      // D1^2 f_K / h      (the 3-halo term reads P h / f_K)
-  NF_D1SQFNS2,  // D1^2 f_n s^2 f_K / h
+  NF_D1SQ,      // D1^2
+  NF_D1SQFNS2,  // D1^2 f_n s^2
   NF_GNS,       // g_n s
   NF_HNS2,      // h_n s^2
   NF_L2MN, NF_L2NN,  // log2 m_n, log2 n_n

@@ -42,13 +42,12 @@ struct Map3Policy {
   static constexpr int NPG = NNODE / G;    // nodes per group
   static constexpr int CH = 8;             // regions per evaluation chunk
   // Point records are read by consecutive threads for consecutive points, so
-  // the FP32 record has an odd number of 32-bit words (21): conflict-free
+  // the FP32 record has an odd number of 32-bit words (17): conflict-free
   // shared-memory banks. FP32 keeps the filter product as its log2.
   struct RecF {
     TriF tri;
     float lo;  // log2(l1 l2 uHat uHat uHat)
     int live;
-    float pad;
   };
   struct RecD {
     Tri<double> tri;

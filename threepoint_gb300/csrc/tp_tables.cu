@@ -565,8 +565,8 @@ TP_TABLE_KERNEL k_node_coefs(const CosmoDev* cos, const TablesDev* tab, double* 
     f[NF_ALA] = v[NC_ALA];
     f[NF_ALD] = v[NC_ALD];
     f[NF_BETAB] = v[NC_BETAB];
-    f[NF_D1SQ] = D1 * D1 / hf;
-    f[NF_D1SQFNS2] = D1 * D1 * v[NC_FN] * sq * sq / hf;
+    f[NF_D1SQ] = D1 * D1;
+    f[NF_D1SQFNS2] = D1 * D1 * v[NC_FN] * sq * sq;
     f[NF_GNS] = v[NC_GN] * sq;
     f[NF_HNS2] = v[NC_HN] * sq * sq;
     f[NF_L2MN] = LOG2_10 * (-2.605 - 2.434 * ls + 5.71 * ls * ls);
@@ -666,9 +666,8 @@ TP_TABLE_KERNEL k_finish(const CosmoDev* cos, const EHConst* eh, const TablesDev
   }
 }
 
-// D = kk P_lin(kk) on the FP32 interpolation grid (log2 kk, kk = k h, uniform on
-// [PLT_LO, PLT_HI]) and its Catmull-Rom cubic per interval i:
-// y(i + f) = y0 + f (c1 + f (c2 + f c3))
+// log2 P_lin on the FP32 interpolation grid (log2(k h) uniform on [PLT_LO, PLT_HI])
+// and its Catmull-Rom cubic per interval i: y(i + f) = y0 + f (c1 + f (c2 + f c3))
 TP_TABLE_KERNEL k_plin_table(const CosmoDev* cos, const EHConst* eh, float4* plt, CosmoK<float>* ck32, int n) {
   // block b of a cosmology builds intervals [b * PLT_SLICE, (b + 1) * PLT_SLICE)
   constexpr int PLT_SLICE = 128;
@@ -676,14 +675,14 @@ TP_TABLE_KERNEL k_plin_table(const CosmoDev* cos, const EHConst* eh, float4* plt
   if (ci >= n) return;
   const CosmoDev c = cos[ci];
   const EHConst e = eh[ci];
-  // y[m] = kk P at grid point m - 1, m = 0 .. PLT_N + 1; this slice needs
+  // y[m] = log2 P at grid point m - 1, m = 0 .. PLT_N + 1; this slice needs
   // y[a .. a + PLT_SLICE + 3]
   __shared__ double y[PLT_SLICE + 4];
   for (int k = threadIdx.x; k < PLT_SLICE + 4; k += blockDim.x) {
     const int m = a + k;
     if (m > PLT_N + 1) continue;
     double kk = exp2(PLT_LO + (m - 1) * (PLT_HI - PLT_LO) / (PLT_N - 1));
-    y[k] = kk * eh_linear_pk(e, kk / c.h);
+    y[k] = log2(eh_linear_pk(e, kk / c.h));
   }
   __syncthreads();
   for (int u = threadIdx.x; u < PLT_SLICE; u += blockDim.x) {
