@@ -7,8 +7,8 @@
  *   void* setup(cosmosis::DataBlock* o)          -> tp_module_setup(&table_of(o), 0, &m)
  *   DATABLOCK_STATUS execute(DataBlock* b, void* m) -> tp_module_execute(m, &table_of(b))
  *   void cleanup(void* m)                        -> tp_module_cleanup(m)
- * where table_of fills tp_datablock with adapters around DataBlock::get_val /
- * put_val (INTEGRATION.md shows them).
+ * where table_of fills tp_datablock with adapters that call DataBlock::get_val
+ * and DataBlock::put_val for the section, key and type each callback names.
  *
  * Keys read and written are the reference's:
  *   setup:   [threepoint] nz_file, zMax, theta_unit, theta_min, theta_max,
