@@ -74,9 +74,12 @@ def test_gamma_rejects_invalid_triangles(gpu_ctx):
 def test_gamma_region_cap_escalation_matches_oracle(nz256, oracle_tables):
     """A flat small triangle of the calculateGamma grid (r = 0.178', u = 0.05,
     v = 0.7: about 15600 regions for Gamma^0) on a context whose region cap is
-    1024: the integral reaches the cap, is integrated again with larger caps
-    until it converges, as the reference's unbounded hcubature_v does, and
-    matches the oracle."""
+    1024: the integral reaches the cap and is integrated again with larger caps
+    until it converges, as the reference's unbounded hcubature_v does. The
+    result is bit for bit the one of a single run with a cap large enough, and
+    agrees with the oracle to 1e-4 (both converged to the requested 1e-3; for
+    ~15000 regions, near-tied region errors that round differently in the two
+    FP64 integrand forms can pick different splits)."""
     import threepoint_gb300 as tp
     from conftest import COSMO1
 
@@ -86,8 +89,11 @@ def test_gamma_region_cap_escalation_matches_oracle(nz256, oracle_tables):
     x = (0.7 * r3 + r2, r2, r3)
     ref = oracle_tables.gamma(0, *x)[0]
     with tp.Context(0) as ctx:
-        ctx.set_limits(region_cap=1024)
         ctx.set_cosmology(tp.cosmology(**COSMO1), nz256)
+        ctx.set_limits(region_cap=65536)
+        once = ctx.gamma_batch([x], comp_mask=1, precision=0)[0, 0]
+        ctx.set_limits(region_cap=1024)
         got = ctx.gamma_batch([x], comp_mask=1, precision=0)[0, 0]
         assert ctx.last_gamma_status[0] == 0
-    assert abs(got - ref) <= 1e-6 * abs(ref), (got, ref)
+    assert got == once
+    assert abs(got - ref) <= 1e-4 * abs(ref), (got, ref)

@@ -1,10 +1,11 @@
 """Autotuner of the <Map^3> kernel's launch shape.
 
-The FP32 kernel k_map3<float> has three build-time knobs (tp_map3.cu):
-TP_MAP3_MINB (CTAs per SM requested from the register allocator: 3 -> 80
-registers per thread, 2 -> 128), TP_MAP3_UNROLL (node pairs per loop
-iteration) and TP_MAP3_DUP_IN_LOOP (triangle pairs held in registers or formed
-at use). The tuner builds the library for every candidate, times the kernel on
+The FP32 kernel k_map3<float> has four build-time knobs (tp_map3.cu):
+TP_MAP3_MINB (CTAs per SM requested from the register allocator: 4 -> 64
+registers per thread, 3 -> 80, 2 -> 128), TP_MAP3_UNROLL (node pairs per loop
+iteration), TP_MAP3_DUP_IN_LOOP (triangle pairs held in registers or formed
+at use) and TP_MAP3_PLT_GLOBAL (linear-P(k) table in shared memory or read
+through L1; the latter is what lets four CTAs fit an SM). The tuner builds the library for every candidate, times the kernel on
 a fixed batch (16 seeded cosmologies x 220 aperture-radius triplets, FP32,
 device-resident, CUDA events, best of 3 launches after a warm-up), writes the
 fastest to threepoint_gb300/tuned.json and rebuilds with it. build() passes
@@ -27,7 +28,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 TUNED = os.path.join(HERE, "tuned.json")
 ARCMIN = 2.9088820866e-4
-KNOBS = {"TP_MAP3_MINB": (3, 2), "TP_MAP3_UNROLL": (1, 2), "TP_MAP3_DUP_IN_LOOP": (1, 0)}
+KNOBS = {"TP_MAP3_MINB": (3, 2), "TP_MAP3_UNROLL": (1, 2), "TP_MAP3_DUP_IN_LOOP": (1, 0), "TP_MAP3_PLT_GLOBAL": (0,)}
 
 
 def _workload(n_cosmo=16, seed=20261203):
@@ -75,12 +76,13 @@ def measure(device=0):
     return best
 
 
-def sweep(device=0):
+def sweep(device=0, knobs=None):
     from threepoint_gb300 import build as B
 
     results = []
-    for vals in itertools.product(*KNOBS.values()):
-        cfg = dict(zip(KNOBS, vals))
+    knobs = knobs or KNOBS
+    for vals in itertools.product(*knobs.values()):
+        cfg = dict(zip(knobs, vals))
         flags = [f"-D{k}={v}" for k, v in cfg.items()]
         B.build(force=True, extra=flags, use_tuned=False)
         r = subprocess.run([sys.executable, "-m", "threepoint_gb300.autotune", "--measure", "--device", str(device)],
@@ -111,11 +113,12 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--measure", action="store_true")
     ap.add_argument("--device", type=int, default=0)
+    ap.add_argument("--knobs", default="", help='JSON {"TP_MAP3_MINB": [3, 4], ...} replacing the default candidates')
     a = ap.parse_args()
     if a.measure:
         print(json.dumps({"ms": measure(a.device)}))
     else:
-        doc = sweep(a.device)
+        doc = sweep(a.device, json.loads(a.knobs) if a.knobs else None)
         print(json.dumps({"best": doc["k_map3"]}))
 
 

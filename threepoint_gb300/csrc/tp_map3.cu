@@ -31,6 +31,12 @@
 #ifndef TP_MAP3_DUP_IN_LOOP
 #define TP_MAP3_DUP_IN_LOOP 1
 #endif
+// 1: the FP32 linear-P(k) table is read from global memory through L1 instead
+// of being staged in shared memory (16 KB less per CTA, so four 256-thread
+// CTAs fit an SM's shared memory)
+#ifndef TP_MAP3_PLT_GLOBAL
+#define TP_MAP3_PLT_GLOBAL 0
+#endif
 #define TP_PRAGMA(x) _Pragma(#x)
 #define TP_UNROLL(n) TP_PRAGMA(unroll n)
 
@@ -60,7 +66,7 @@ struct Map3Policy {
   static constexpr int PD = 1;
   static constexpr int NS = 1;
   __device__ static int slot(int) { return 0; }
-  static constexpr size_t PLT_BYTES = sizeof(R) == 4 ? sizeof(float4) * PLT_N : 0;
+  static constexpr size_t PLT_BYTES = (sizeof(R) == 4 && !TP_MAP3_PLT_GLOBAL) ? sizeof(float4) * PLT_N : 0;
   static constexpr size_t PSMEM = sizeof(R) * NCP * NNODE + sizeof(CosmoK<R>) + sizeof(BulkBar) + 128 + PLT_BYTES;
 
   // inputs
@@ -111,7 +117,7 @@ struct Map3Policy {
         *s_ck = ck[c];
       }
       __syncthreads();
-      if constexpr (sizeof(R) == 4) {
+      if constexpr (sizeof(R) == 4 && !TP_MAP3_PLT_GLOBAL) {
         // the FP32 linear-P(k) table follows the node table into shared memory
         const float4* gp = reinterpret_cast<const float4*>(s_ck->plt);
         if (gp) {
