@@ -745,6 +745,42 @@ def run_apm(args):
                    "d2h_bytes_per_step": 8 * ntrip},
            "gpu_launches": (6 + 2 * len(thetas)) * args.steps, "gpu_launches_note": "this library's kernels; cuFFT's transforms (3 + 2 per aperture per step) in addition", "clocks": clocks,
            "device_vs_host_api_max_rel": float(np.max(np.abs(host - gpu_vals)) / np.max(np.abs(gpu_vals)))}
+    # the same pipeline with FP32 transforms and Fourier products (gridding,
+    # maps and sums FP64), device-resident, against the FP64 values
+    plan32 = G._Plan(ctx, npix, fs, thetas, False, precision=tp.FP32)
+    out32 = torch.zeros_like(out)
+
+    def step32():
+        rc = L.tp_apm_extract_map3_device(plan32._h, dx.data_ptr(), dy.data_ptr(), d1.data_ptr(), d2.data_ptr(),
+                                          n_gal, 1, out32.data_ptr())
+        if rc:
+            raise RuntimeError(L.tp_last_error(ctx._h).decode())
+
+    for _ in range(args.warmup):
+        step32()
+    torch.cuda.synchronize()
+    e0.record(st)
+    for _ in range(args.steps):
+        step32()
+    e1.record(st)
+    torch.cuda.synchronize()
+    t32 = e0.elapsed_time(e1) * 1e-3
+    v32 = out32.cpu().numpy()
+    r32 = np.abs(v32 - gpu_vals) / np.abs(gpu_vals)
+    res["fp32_transforms"] = {"value": args.steps / t32, "unit": "fields/s", "ms_per_step": t32 / args.steps * 1e3,
+                              "max_rel_vs_fp64": float(r32.max()), "median_rel_vs_fp64": float(np.median(r32)),
+                              "outputs": int(r32.size)}
+    plan32.close()
+    # FP64 transforms: 5 F^2 log2(F^2) flop each, 3 + 2 per aperture per field
+    F = int(L.tp_apm_fft_size(plan._h))
+    flops = (3 + 2 * len(thetas)) * 5.0 * F * F * math.log2(F * F)
+    f64_peak = tp.pipe_peaks(local)[2] * 2
+    res["roofline"] = {"bound": "fp64", "achieved": flops / (t_dev / args.steps) / 1e12, "peak": f64_peak / 1e12,
+                       "unit": "TFLOP/s", "frac": flops / (t_dev / args.steps) / f64_peak, "traffic": None,
+                       "kernel": "the field's FP64 2-D transforms (cuFFT, 88% of the device time) and this "
+                                 "library's kernels around them",
+                       "work": "5 F^2 log2(F^2) flop per F x F transform",
+                       "peak_source": "tp_pipe_peaks FP64 FMA/s x 2, measured now"}
     if not args.no_cpu_baseline:
         from oracle import aperture_mass as A
 

@@ -269,10 +269,13 @@ int tp_gamma_batch(tp_ctx* ctx, int cosmo_index, const double* x, int n, int com
  * filter (polynomial != 0: Schneider's polynomial filter, else the
  * exponential one); it keeps on the device the Fourier transforms of the filter
  * grids of every aperture, so only the field's own transforms are done per
- * field. Needs cuFFT at run time (loaded with dlopen; TP_ERR_STATE if absent). */
+ * field. precision TP_FP64 does the transforms and Fourier products in FP64
+ * (the reference's numpy precision); TP_FP32 does them in FP32 (gridding, maps
+ * and the <Map^3> sums stay FP64). Needs cuFFT at run time (loaded with
+ * dlopen; TP_ERR_STATE if absent). */
 typedef struct tp_apm tp_apm;
 int tp_apm_create(tp_ctx* ctx, int npix, double fieldsize, const double* thetas, int n_theta, int polynomial,
-                  tp_apm** out);
+                  int precision, tp_apm** out);
 /* A tp_apm's calls need its context; destroying it does not (it may come
  * after tp_ctx_destroy). */
 int tp_apm_destroy(tp_apm* apm);

@@ -112,3 +112,25 @@ def test_gpu_rejects_unsupported_options():
             ac.Map_fft(np.zeros((32, 32), complex))
         with pytest.raises(tp.ThreepointError):
             tp.aperture_mass._Plan(ctx, 32, 20.0, [0.0], False)
+
+
+@pytest.mark.gpu
+def test_gpu_fp32_transforms_against_fp64():
+    """FP32 transforms and Fourier products (gridding, maps and sums in FP64)
+    against the FP64 pipeline: maps within 1e-5 of their largest value, <Map^3>
+    within 1e-3."""
+    tp, G = _gpu()
+    rng = np.random.default_rng(9)
+    n, fs, th = 128, 60.0, [1.0, 2.0, 4.0]
+    x, y = rng.uniform(0, fs, 20000), rng.uniform(0, fs, 20000)
+    g = 0.05 * np.exp(2j * np.pi * (x / 13.0 + y / 29.0)) + 0.3 * (rng.standard_normal(20000) +
+                                                                  1j * rng.standard_normal(20000))
+    with tp.Context(0) as ctx:
+        p64 = G._Plan(ctx, n, fs, th, False, precision=0)
+        p32 = G._Plan(ctx, n, fs, th, False, precision=1)
+        p64.grid(x, y, g)
+        p32.grid(x, y, g)
+        m64, m32 = p64.maps(), p32.maps()
+        assert rel(m32, m64) < 1e-5
+        v64, v32 = p64.map3(True), p32.map3(True)
+        assert np.max(np.abs(v32 - v64) / np.abs(v64)) < 1e-3

@@ -157,7 +157,7 @@ def lib():
         L.tp_pell_batch.argtypes = [p, i, dp, l, i, dp]
         L.tp_bkappa_nodes.argtypes = [p, i, dp, l, i, dp, dp]
         L.tp_gamma_integrand_points.argtypes = [p, i, dp, i, dp, i, i, dp]
-        L.tp_apm_create.argtypes = [p, i, d, dp, i, i, C.POINTER(p)]
+        L.tp_apm_create.argtypes = [p, i, d, dp, i, i, i, C.POINTER(p)]
         L.tp_apm_destroy.argtypes = [p]
         L.tp_apm_fft_size.argtypes = [p]
         L.tp_apm_grid.argtypes = [p, dp, dp, dp, dp, l]

@@ -33,10 +33,12 @@ def _arr(x):
 
 class _Plan:
     """One tp_apm: grid, field, apertures and filter, with the filters'
-    Fourier transforms kept on the device."""
+    Fourier transforms kept on the device; precision 0 (FP64, the default) or
+    1 (FP32 transforms and Fourier products)."""
 
-    def __init__(self, ctx: Context, npix, fieldsize, thetas, polynomial):
+    def __init__(self, ctx: Context, npix, fieldsize, thetas, polynomial, precision=0):
         self.ctx = ctx
+        self.precision = int(precision)
         self.npix = int(npix)
         self.fieldsize = float(fieldsize)
         self.thetas = [float(t) for t in thetas]
@@ -44,7 +46,7 @@ class _Plan:
         self._h = C.c_void_p(0)
         th = _arr(self.thetas)
         _check(ctx._h, lib().tp_apm_create(ctx._h, self.npix, self.fieldsize, _dp(th), len(th), int(polynomial),
-                                           C.byref(self._h)))
+                                           self.precision, C.byref(self._h)))
         ctx._adopt(self)
 
     def close(self):

@@ -13,11 +13,14 @@
 // so a field costs three forward transforms (the shear grid's real and
 // imaginary parts and the weight grid) and two inverse ones per aperture
 // (numerator Im(g) * Im(Q) - Re(g) * Re(Q) and denominator w * |Q| multiplied
-// in Fourier space by one fused kernel). The 2-D FFTs are cuFFT's (FP64,
-// loaded at run time with dlopen so that the rest of the library does not
-// depend on it); gridding, filters, spectral products, the crop/divide and
-// the triplet reduction are this file's kernels. The triplet reduction reads
-// each pixel's n_theta map values once and accumulates all triplets.
+// in Fourier space by one fused kernel). The 2-D FFTs are cuFFT's (loaded at
+// run time with dlopen so that the rest of the library does not depend on
+// it), in FP64 (TP_FP64, the reference's numpy precision) or FP32 (TP_FP32:
+// transforms, filter spectra and Fourier products in FP32; gridding, maps and
+// the triplet sums stay FP64); gridding, filters, spectral products, the
+// crop/divide and the triplet reduction are this file's kernels. The triplet
+// reduction reads each pixel's n_theta map values once and accumulates all
+// triplets.
 #include <cuda_runtime.h>
 #include <cufft.h>
 #include <dlfcn.h>
@@ -39,6 +42,8 @@ struct CufftApi {
   cufftResult (*plan2d)(cufftHandle*, int, int, cufftType) = nullptr;
   cufftResult (*exec_d2z)(cufftHandle, cufftDoubleReal*, cufftDoubleComplex*) = nullptr;
   cufftResult (*exec_z2d)(cufftHandle, cufftDoubleComplex*, cufftDoubleReal*) = nullptr;
+  cufftResult (*exec_r2c)(cufftHandle, cufftReal*, cufftComplex*) = nullptr;
+  cufftResult (*exec_c2r)(cufftHandle, cufftComplex*, cufftReal*) = nullptr;
   cufftResult (*set_stream)(cufftHandle, cudaStream_t) = nullptr;
   cufftResult (*destroy)(cufftHandle) = nullptr;
 };
@@ -58,9 +63,12 @@ const CufftApi& cufft() {
     api.plan2d = (decltype(api.plan2d))dlsym(h, "cufftPlan2d");
     api.exec_d2z = (decltype(api.exec_d2z))dlsym(h, "cufftExecD2Z");
     api.exec_z2d = (decltype(api.exec_z2d))dlsym(h, "cufftExecZ2D");
+    api.exec_r2c = (decltype(api.exec_r2c))dlsym(h, "cufftExecR2C");
+    api.exec_c2r = (decltype(api.exec_c2r))dlsym(h, "cufftExecC2R");
     api.set_stream = (decltype(api.set_stream))dlsym(h, "cufftSetStream");
     api.destroy = (decltype(api.destroy))dlsym(h, "cufftDestroy");
-    api.ok = api.plan2d && api.exec_d2z && api.exec_z2d && api.set_stream && api.destroy;
+    api.ok = api.plan2d && api.exec_d2z && api.exec_z2d && api.exec_r2c && api.exec_c2r && api.set_stream &&
+             api.destroy;
     if (!api.ok) api.why = "libcufft lacks a needed symbol";
   });
   return api;
@@ -129,9 +137,10 @@ __global__ void k_apm_cic(const double* __restrict__ x, const double* __restrict
 // q = Q(r) conj(z)^2 / |z|^2 (0 at z = 0) with Q the exponential filter
 // (r/t)^2 / (4 pi t^2) exp(-(r/t)^2 / 2) or the polynomial one
 // 6 / pi (r/t)^4 (1 - (r/t)^4) / t^2 inside r <= t. Writes Re q, Im q and |q|
-// into the top-left npix x npix corner of three zero-padded F x F grids.
-__global__ void k_apm_filter(int npix, int F, double fieldsize, double theta, int polynomial, double* qr, double* qi,
-                             double* qa) {
+// into the top-left npix x npix corner of three zero-padded F x F grids
+// (computed in FP64, stored in T).
+template <typename T>
+__global__ void k_apm_filter(int npix, int F, double fieldsize, double theta, int polynomial, T* qr, T* qi, T* qa) {
   const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= (long)npix * npix) return;
   const int i = (int)(t / npix), j = (int)(t % npix);
@@ -152,79 +161,94 @@ __global__ void k_apm_filter(int npix, int F, double fieldsize, double theta, in
     ab = sqrt(re * re + im * im);
   }
   const size_t o = (size_t)i * F + j;
-  qr[o] = re;
-  qi[o] = im;
-  qa[o] = ab;
+  qr[o] = (T)re;
+  qi[o] = (T)im;
+  qa[o] = (T)ab;
 }
 
 // U filter grid of one aperture (Ufunc/Ufunc_array, :72-114), exponential
 // filter: U(r) = exp(-x) (1 - x) / (2 pi theta^2), x = (r/theta)^2 / 2
-__global__ void k_apm_ufilter(int npix, int F, double fieldsize, double theta, double* u) {
+template <typename T>
+__global__ void k_apm_ufilter(int npix, int F, double fieldsize, double theta, T* u) {
   const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= (long)npix * npix) return;
   const int i = (int)(t / npix), j = (int)(t % npix);
   const double zr = i - npix / 2.0, zi = j - npix / 2.0;
   const double r = sqrt(zr * zr + zi * zi) * fieldsize / npix;
   const double xh = (r / theta) * (r / theta) / 2;
-  u[(size_t)i * F + j] = exp(-xh) * (1. - xh) / (2 * PI) / (theta * theta);
+  u[(size_t)i * F + j] = (T)(exp(-xh) * (1. - xh) / (2 * PI) / (theta * theta));
 }
 
-// spectrum product a * b (complex), n entries
-__global__ void k_apm_mul(const double2* __restrict__ a, const double2* __restrict__ b, long n, double2* c) {
+// spectrum product a * b (complex, C = double2 or float2), n entries
+template <typename C>
+__global__ void k_apm_mul(const C* __restrict__ a, const C* __restrict__ b, long n, C* c) {
   const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= n) return;
-  const double2 x = a[t], y = b[t];
-  c[t] = make_double2(x.x * y.x - x.y * y.y, x.x * y.y + x.y * y.x);
+  const C x = a[t], y = b[t];
+  C r;
+  r.x = x.x * y.x - x.y * y.y;
+  r.y = x.x * y.y + x.y * y.x;
+  c[t] = r;
 }
 
 // 'same'-mode window of an unnormalised inverse transform times scale
-__global__ void k_apm_crop_scaled(const double* __restrict__ v, int npix, int F, double scale, double* map) {
+template <typename T>
+__global__ void k_apm_crop_scaled(const T* __restrict__ v, int npix, int F, double scale, double* map) {
   const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= (long)npix * npix) return;
   const int off = (npix - 1) / 2;
   const int i = (int)(t / npix), j = (int)(t % npix);
-  map[t] = v[(size_t)(i + off) * F + (j + off)] * scale;
+  map[t] = (double)v[(size_t)(i + off) * F + (j + off)] * scale;
 }
 
 // copies an npix x npix grid into the top-left corner of a zeroed F x F grid
-__global__ void k_apm_pad(const double* __restrict__ src, int npix, int F, double* dst) {
+template <typename T>
+__global__ void k_apm_pad(const double* __restrict__ src, int npix, int F, T* dst) {
   const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= (long)npix * npix) return;
   const int i = (int)(t / npix), j = (int)(t % npix);
-  dst[(size_t)i * F + j] = src[t];
+  dst[(size_t)i * F + j] = (T)src[t];
 }
 
 // Fourier-space products of one aperture: num = Im(g) Im(Q) - Re(g) Re(Q),
 // den = w |Q| (Map_fft :211-236 with norm_fft :283-286), cross (optional) =
 // -(Re(g) Im(Q) + Im(g) Re(Q)) (return_mcross :246-255)
-__global__ void k_apm_spectra(const double2* __restrict__ Yr, const double2* __restrict__ Yi,
-                              const double2* __restrict__ W, const double2* __restrict__ Qr,
-                              const double2* __restrict__ Qi, const double2* __restrict__ Qa, long n, double2* num,
-                              double2* den, double2* cross) {
+template <typename C>
+__global__ void k_apm_spectra(const C* __restrict__ Yr, const C* __restrict__ Yi, const C* __restrict__ W,
+                              const C* __restrict__ Qr, const C* __restrict__ Qi, const C* __restrict__ Qa, long n,
+                              C* num, C* den, C* cross) {
   const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= n) return;
-  const double2 yr = Yr[t], yi = Yi[t], w = W[t], qr = Qr[t], qi = Qi[t], qa = Qa[t];
-  num[t] = make_double2(yi.x * qi.x - yi.y * qi.y - (yr.x * qr.x - yr.y * qr.y),
-                        yi.x * qi.y + yi.y * qi.x - (yr.x * qr.y + yr.y * qr.x));
-  den[t] = make_double2(w.x * qa.x - w.y * qa.y, w.x * qa.y + w.y * qa.x);
-  if (cross)
-    cross[t] = make_double2(-(yr.x * qi.x - yr.y * qi.y + yi.x * qr.x - yi.y * qr.y),
-                            -(yr.x * qi.y + yr.y * qi.x + yi.x * qr.y + yi.y * qr.x));
+  const C yr = Yr[t], yi = Yi[t], w = W[t], qr = Qr[t], qi = Qi[t], qa = Qa[t];
+  C a, b;
+  a.x = yi.x * qi.x - yi.y * qi.y - (yr.x * qr.x - yr.y * qr.y);
+  a.y = yi.x * qi.y + yi.y * qi.x - (yr.x * qr.y + yr.y * qr.x);
+  b.x = w.x * qa.x - w.y * qa.y;
+  b.y = w.x * qa.y + w.y * qa.x;
+  num[t] = a;
+  den[t] = b;
+  if (cross) {
+    C c;
+    c.x = -(yr.x * qi.x - yr.y * qi.y + yi.x * qr.x - yi.y * qr.y);
+    c.y = -(yr.x * qi.y + yr.y * qi.x + yi.x * qr.y + yi.y * qr.x);
+    cross[t] = c;
+  }
 }
 
 // the 'same'-mode window of the linear convolution (rows and columns
 // off .. off + npix - 1, off = (npix - 1) / 2): map = num / den (the inverse
 // transforms' common 1/F^2 cancels); cross / den likewise
-__global__ void k_apm_crop(const double* __restrict__ num, const double* __restrict__ den,
-                           const double* __restrict__ cross, int npix, int F, double* map, double* mcross) {
+template <typename T>
+__global__ void k_apm_crop(const T* __restrict__ num, const T* __restrict__ den, const T* __restrict__ cross,
+                           int npix, int F, double* map, double* mcross) {
   const long t = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= (long)npix * npix) return;
   const int off = (npix - 1) / 2;
   const int i = (int)(t / npix), j = (int)(t % npix);
   const size_t o = (size_t)(i + off) * F + (j + off);
-  const double d = den[o];
-  map[t] = num[o] / d;
-  if (cross && mcross) mcross[t] = cross[o] / d;
+  const double d = (double)den[o];
+  map[t] = (double)num[o] / d;
+  if (cross && mcross) mcross[t] = (double)cross[o] / d;
 }
 
 // <Map^3> of every triplet i <= j <= k (extract_Map3_of_field :466-531): the
@@ -287,6 +311,8 @@ struct tp_apm {
   tp_ctx* ctx = nullptr;  // must outlive the tp_apm's calls (not its destruction)
   int device = 0;
   int npix = 0, F = 0, n_theta = 0, polynomial = 0;
+  int precision = TP_FP64;  // of the transforms and Fourier products
+  size_t rsz = sizeof(double), csz = sizeof(double2);  // bytes of one real / complex transform value
   double fieldsize = 0;
   std::vector<double> thetas;
   std::string err;
@@ -296,13 +322,14 @@ struct tp_apm {
   // device state
   double* edges = nullptr;                          // [npix + 1]
   double *g_re = nullptr, *g_im = nullptr, *g_w = nullptr;  // CIC grids [npix][npix]
-  double* pad = nullptr;                            // [3][F][F] padded real grids
-  double2* spec = nullptr;                          // [3][F][F/2+1]: Re g, Im g, w
-  double2* qspec = nullptr;                         // [n_theta][3][F][F/2+1]: Re Q, Im Q, |Q|
-  double2* work = nullptr;                          // [3][F][F/2+1]: num, den, cross
+  // transform buffers, in the precision's real / complex type
+  char* pad = nullptr;                              // [3][F][F] padded real grids
+  char* spec = nullptr;                             // [3][F][F/2+1]: Re g, Im g, w
+  char* qspec = nullptr;                            // [n_theta][3][F][F/2+1]: Re Q, Im Q, |Q|
+  char* work = nullptr;                             // [3][F][F/2+1]: num, den, cross
   double* maps = nullptr;                           // [n_theta][npix][npix]
   double* mcross = nullptr;                         // [n_theta][npix][npix] (allocated on demand)
-  double2* uspec = nullptr;                         // [n_theta][F][F/2+1] U filter spectra (on demand)
+  char* uspec = nullptr;                            // [n_theta][F][F/2+1] U filter spectra (on demand)
   double* sums = nullptr;                           // [n_trip]
   double* counts = nullptr;                         // [n_trip]
   double* outv = nullptr;                           // [n_trip]
@@ -310,6 +337,8 @@ struct tp_apm {
   int* cut_same = nullptr;                          // [n_theta]
   std::vector<int> h_cut, h_cut_same;
   int n_trip() const { return n_theta * (n_theta + 1) * (n_theta + 2) / 6; }
+  char* R(char* base, size_t q) const { return base + q * nreal * rsz; }  // q-th real grid
+  char* Cx(char* base, size_t q) const { return base + q * ncplx * csz; }  // q-th spectrum
 };
 
 namespace {
@@ -328,6 +357,21 @@ int apm_fft(tp_apm* a, cufftResult r, const char* where) {
   return apm_fail(a, TP_ERR_CUDA, std::string(where) + ": cuFFT error " + std::to_string((int)r));
 }
 
+int fwd_fft(tp_apm* a, char* in, char* out) {
+  const CufftApi& api = cufft();
+  const cufftResult r = a->precision == TP_FP64
+                            ? api.exec_d2z(a->fwd, (cufftDoubleReal*)in, (cufftDoubleComplex*)out)
+                            : api.exec_r2c(a->fwd, (cufftReal*)in, (cufftComplex*)out);
+  return apm_fft(a, r, "forward FFT");
+}
+int inv_fft(tp_apm* a, char* in, char* out) {
+  const CufftApi& api = cufft();
+  const cufftResult r = a->precision == TP_FP64
+                            ? api.exec_z2d(a->inv, (cufftDoubleComplex*)in, (cufftDoubleReal*)out)
+                            : api.exec_c2r(a->inv, (cufftComplex*)in, (cufftReal*)out);
+  return apm_fft(a, r, "inverse FFT");
+}
+
 // border of extract_Map3_of_field (:492-503): int(round(theta / fieldsize *
 // npix * f)), f = 4 for the exponential filter (99.8 % of its power inside
 // 4 theta), 1 for the polynomial one; numpy rounds halves to even
@@ -337,47 +381,73 @@ int border(double theta, double fieldsize, int npix, int polynomial) {
 }
 
 // the per-field part: forward transforms of the three grids, then per
-// aperture the products, two (three) inverse transforms and the crop
-int apm_maps_device(tp_apm* a, bool want_cross) {
-  const CufftApi& api = cufft();
+// aperture the products, two (three) inverse transforms and the crop; T / C
+// the real / complex type of the transforms
+template <typename T, typename C>
+int apm_maps_t(tp_apm* a, bool want_cross) {
   cudaStream_t s = a->ctx->stream;
   const int n = a->npix, F = a->F;
   const long npx = (long)n * n;
-  cudaError_t e = cudaMemsetAsync(a->pad, 0, sizeof(double) * 3 * a->nreal, s);
+  cudaError_t e = cudaMemsetAsync(a->pad, 0, a->rsz * 3 * a->nreal, s);
   if (e != cudaSuccess) return apm_cuda(a, e, "apm pad clear");
   const double* src[3] = {a->g_re, a->g_im, a->g_w};
-  for (int q = 0; q < 3; ++q) k_apm_pad<<<blocks_for(npx, 256), 256, 0, s>>>(src[q], n, F, a->pad + q * a->nreal);
+  for (int q = 0; q < 3; ++q) k_apm_pad<T><<<blocks_for(npx, 256), 256, 0, s>>>(src[q], n, F, (T*)a->R(a->pad, q));
   e = cudaGetLastError();
   if (e != cudaSuccess) return apm_cuda(a, e, "apm pad");
   for (int q = 0; q < 3; ++q) {
-    int st = apm_fft(a, api.exec_d2z(a->fwd, a->pad + q * a->nreal, (cufftDoubleComplex*)(a->spec + q * a->ncplx)),
-                     "forward FFT");
+    int st = fwd_fft(a, a->R(a->pad, q), a->Cx(a->spec, q));
     if (st) return st;
   }
   if (want_cross && !a->mcross) {
     e = cudaMalloc(&a->mcross, sizeof(double) * a->n_theta * npx);
     if (e != cudaSuccess) return apm_cuda(a, e, "apm cross maps");
   }
+  const C* Y = (const C*)a->spec;
   for (int t = 0; t < a->n_theta; ++t) {
-    const double2* Q = a->qspec + (size_t)t * 3 * a->ncplx;
-    double2* cross = want_cross ? a->work + 2 * a->ncplx : nullptr;
-    k_apm_spectra<<<blocks_for((long)a->ncplx, 256), 256, 0, s>>>(a->spec, a->spec + a->ncplx, a->spec + 2 * a->ncplx, Q,
-                                                                 Q + a->ncplx, Q + 2 * a->ncplx, (long)a->ncplx,
-                                                                 a->work, a->work + a->ncplx, cross);
+    const C* Q = (const C*)a->Cx(a->qspec, 3 * (size_t)t);
+    C* W = (C*)a->work;
+    const long nc = (long)a->ncplx;
+    k_apm_spectra<C><<<blocks_for(nc, 256), 256, 0, s>>>(Y, Y + nc, Y + 2 * nc, Q, Q + nc, Q + 2 * nc, nc, W, W + nc,
+                                                        want_cross ? W + 2 * nc : nullptr);
     e = cudaGetLastError();
     if (e != cudaSuccess) return apm_cuda(a, e, "apm spectra");
     for (int q = 0; q < (want_cross ? 3 : 2); ++q) {
-      int st = apm_fft(a, api.exec_z2d(a->inv, (cufftDoubleComplex*)(a->work + q * a->ncplx), a->pad + q * a->nreal),
-                       "inverse FFT");
+      int st = inv_fft(a, a->Cx(a->work, q), a->R(a->pad, q));
       if (st) return st;
     }
-    k_apm_crop<<<blocks_for(npx, 256), 256, 0, s>>>(a->pad, a->pad + a->nreal, want_cross ? a->pad + 2 * a->nreal : nullptr,
-                                                    n, F, a->maps + (size_t)t * npx,
-                                                    want_cross ? a->mcross + (size_t)t * npx : nullptr);
+    k_apm_crop<T><<<blocks_for(npx, 256), 256, 0, s>>>((const T*)a->R(a->pad, 0), (const T*)a->R(a->pad, 1),
+                                                       want_cross ? (const T*)a->R(a->pad, 2) : nullptr, n, F,
+                                                       a->maps + (size_t)t * npx,
+                                                       want_cross ? a->mcross + (size_t)t * npx : nullptr);
     e = cudaGetLastError();
     if (e != cudaSuccess) return apm_cuda(a, e, "apm crop");
   }
   return TP_OK;
+}
+
+int apm_maps_device(tp_apm* a, bool want_cross) {
+  return a->precision == TP_FP64 ? apm_maps_t<double, double2>(a, want_cross) : apm_maps_t<float, float2>(a, want_cross);
+}
+
+// the Fourier transforms of the Q filter grids of every aperture
+template <typename T>
+int apm_filters_t(tp_apm* a) {
+  cudaStream_t s = a->ctx->stream;
+  const long npx = (long)a->npix * a->npix;
+  for (int t = 0; t < a->n_theta; ++t) {
+    cudaError_t e = cudaMemsetAsync(a->pad, 0, a->rsz * 3 * a->nreal, s);
+    if (e != cudaSuccess) return apm_cuda(a, e, "apm filter clear");
+    k_apm_filter<T><<<blocks_for(npx, 256), 256, 0, s>>>(a->npix, a->F, a->fieldsize, a->thetas[t], a->polynomial,
+                                                         (T*)a->R(a->pad, 0), (T*)a->R(a->pad, 1),
+                                                         (T*)a->R(a->pad, 2));
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return apm_cuda(a, e, "apm filter");
+    for (int q = 0; q < 3; ++q) {
+      int st = fwd_fft(a, a->R(a->pad, q), a->Cx(a->qspec, 3 * (size_t)t + q));
+      if (st) return st;
+    }
+  }
+  return apm_cuda(a, cudaStreamSynchronize(s), "apm filters");
 }
 
 int apm_map3_device(tp_apm* a, int same_fieldsize) {
@@ -431,10 +501,11 @@ int apm_grid_device(tp_apm* a, const double* x, const double* y, const double* g
 extern "C" int tp_apm_destroy(tp_apm* a);
 
 extern "C" int tp_apm_create(tp_ctx* ctx, int npix, double fieldsize, const double* thetas, int n_theta,
-                             int polynomial, tp_apm** out) {
+                             int polynomial, int precision, tp_apm** out) {
   TpRange nvtx_range("tp_apm_create");
   if (!ctx || !out || !thetas || npix < 8 || !(fieldsize > 0) || n_theta < 1 || n_theta > APM_MAX_THETA)
     return TP_ERR_ARG;
+  if (precision != TP_FP64 && precision != TP_FP32) return TP_ERR_ARG;
   for (int i = 0; i < n_theta; ++i)
     if (!(thetas[i] > 0)) return tp_fail(ctx, TP_ERR_ARG, "aperture radii must be > 0");
   *out = nullptr;
@@ -448,6 +519,9 @@ extern "C" int tp_apm_create(tp_ctx* ctx, int npix, double fieldsize, const doub
   a->fieldsize = fieldsize;
   a->n_theta = n_theta;
   a->polynomial = polynomial ? 1 : 0;
+  a->precision = precision;
+  a->rsz = precision == TP_FP64 ? sizeof(double) : sizeof(float);
+  a->csz = precision == TP_FP64 ? sizeof(double2) : sizeof(float2);
   a->thetas.assign(thetas, thetas + n_theta);
   a->F = fft_size(2 * npix - 1);
   a->nreal = (size_t)a->F * a->F;
@@ -466,10 +540,10 @@ extern "C" int tp_apm_create(tp_ctx* ctx, int npix, double fieldsize, const doub
   M(&a->g_re, sizeof(double) * npx);
   M(&a->g_im, sizeof(double) * npx);
   M(&a->g_w, sizeof(double) * npx);
-  M(&a->pad, sizeof(double) * 3 * a->nreal);
-  M(&a->spec, sizeof(double2) * 3 * a->ncplx);
-  M(&a->qspec, sizeof(double2) * 3 * a->ncplx * n_theta);
-  M(&a->work, sizeof(double2) * 3 * a->ncplx);
+  M(&a->pad, a->rsz * 3 * a->nreal);
+  M(&a->spec, a->csz * 3 * a->ncplx);
+  M(&a->qspec, a->csz * 3 * a->ncplx * n_theta);
+  M(&a->work, a->csz * 3 * a->ncplx);
   M(&a->maps, sizeof(double) * npx * n_theta);
   M(&a->sums, sizeof(double) * nt);
   M(&a->counts, sizeof(double) * nt);
@@ -477,11 +551,12 @@ extern "C" int tp_apm_create(tp_ctx* ctx, int npix, double fieldsize, const doub
   M(&a->cut, sizeof(int) * n_theta);
   M(&a->cut_same, sizeof(int) * n_theta);
   if (e != cudaSuccess) return fail(tp_fail(ctx, TP_ERR_NOMEM, std::string("apm buffers: ") + cudaGetErrorString(e)));
-  if (api.plan2d(&a->fwd, a->F, a->F, CUFFT_D2Z) != CUFFT_SUCCESS)
-    return fail(tp_fail(ctx, TP_ERR_CUDA, "cufftPlan2d D2Z"));
+  const bool f64 = precision == TP_FP64;
+  if (api.plan2d(&a->fwd, a->F, a->F, f64 ? CUFFT_D2Z : CUFFT_R2C) != CUFFT_SUCCESS)
+    return fail(tp_fail(ctx, TP_ERR_CUDA, "cufftPlan2d forward"));
   a->have_fwd = true;
-  if (api.plan2d(&a->inv, a->F, a->F, CUFFT_Z2D) != CUFFT_SUCCESS)
-    return fail(tp_fail(ctx, TP_ERR_CUDA, "cufftPlan2d Z2D"));
+  if (api.plan2d(&a->inv, a->F, a->F, f64 ? CUFFT_Z2D : CUFFT_C2R) != CUFFT_SUCCESS)
+    return fail(tp_fail(ctx, TP_ERR_CUDA, "cufftPlan2d inverse"));
   a->have_inv = true;
   api.set_stream(a->fwd, ctx->stream);
   api.set_stream(a->inv, ctx->stream);
@@ -503,19 +578,8 @@ extern "C" int tp_apm_create(tp_ctx* ctx, int npix, double fieldsize, const doub
     e = cudaMemcpyAsync(a->cut_same, a->h_cut_same.data(), sizeof(int) * n_theta, cudaMemcpyHostToDevice, s);
   if (e != cudaSuccess) return fail(tp_cuda(ctx, e, "apm upload"));
   // the filter spectra of every aperture, computed once
-  for (int t = 0; t < n_theta && e == cudaSuccess; ++t) {
-    e = cudaMemsetAsync(a->pad, 0, sizeof(double) * 3 * a->nreal, s);
-    if (e != cudaSuccess) break;
-    k_apm_filter<<<blocks_for((long)npx, 256), 256, 0, s>>>(npix, a->F, fieldsize, thetas[t], a->polynomial, a->pad,
-                                                           a->pad + a->nreal, a->pad + 2 * a->nreal);
-    e = cudaGetLastError();
-    for (int q = 0; q < 3 && e == cudaSuccess; ++q)
-      if (api.exec_d2z(a->fwd, a->pad + q * a->nreal,
-                       (cufftDoubleComplex*)(a->qspec + ((size_t)t * 3 + q) * a->ncplx)) != CUFFT_SUCCESS)
-        return fail(tp_fail(ctx, TP_ERR_CUDA, "filter FFT"));
-  }
-  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-  if (e != cudaSuccess) return fail(tp_cuda(ctx, e, "apm filters"));
+  const int st = f64 ? apm_filters_t<double>(a) : apm_filters_t<float>(a);
+  if (st) return fail(st);
   *out = a;
   return TP_OK;
 }
@@ -602,51 +666,56 @@ extern "C" int tp_apm_maps(tp_apm* a, double* maps, double* mcross) {
   return apm_cuda(a, e, "apm maps");
 }
 
-extern "C" int tp_apm_maps_from_kappa(tp_apm* a, const double* kappa, double* maps) {
-  TpRange nvtx_range("tp_apm_maps_from_kappa");
-  if (!a || !kappa) return TP_ERR_ARG;
-  cudaSetDevice(a->ctx->device);
-  const CufftApi& api = cufft();
+template <typename T, typename C>
+int apm_kappa_t(tp_apm* a, const double* kappa) {
   cudaStream_t s = a->ctx->stream;
   const int n = a->npix, F = a->F;
   const long npx = (long)n * n;
   cudaError_t e = cudaSuccess;
   if (!a->uspec) {
-    e = cudaMalloc(&a->uspec, sizeof(double2) * a->ncplx * a->n_theta);
+    e = cudaMalloc(&a->uspec, a->csz * a->ncplx * a->n_theta);
     if (e != cudaSuccess) return apm_cuda(a, e, "apm U spectra");
-    for (int t = 0; t < a->n_theta && e == cudaSuccess; ++t) {
-      e = cudaMemsetAsync(a->pad, 0, sizeof(double) * a->nreal, s);
-      if (e != cudaSuccess) break;
-      k_apm_ufilter<<<blocks_for(npx, 256), 256, 0, s>>>(n, F, a->fieldsize, a->thetas[t], a->pad);
+    for (int t = 0; t < a->n_theta; ++t) {
+      e = cudaMemsetAsync(a->pad, 0, a->rsz * a->nreal, s);
+      if (e != cudaSuccess) return apm_cuda(a, e, "apm U filter clear");
+      k_apm_ufilter<T><<<blocks_for(npx, 256), 256, 0, s>>>(n, F, a->fieldsize, a->thetas[t], (T*)a->pad);
       e = cudaGetLastError();
-      if (e == cudaSuccess) {
-        int st = apm_fft(a, api.exec_d2z(a->fwd, a->pad, (cufftDoubleComplex*)(a->uspec + (size_t)t * a->ncplx)),
-                         "U filter FFT");
-        if (st) return st;
-      }
+      if (e != cudaSuccess) return apm_cuda(a, e, "apm U filter");
+      int st = fwd_fft(a, a->pad, a->Cx(a->uspec, t));
+      if (st) return st;
     }
-    if (e != cudaSuccess) return apm_cuda(a, e, "apm U filters");
   }
   // the kappa grid goes through the shear grid's real-part buffer
   e = cudaMemcpyAsync(a->g_re, kappa, sizeof(double) * npx, cudaMemcpyHostToDevice, s);
-  if (e == cudaSuccess) e = cudaMemsetAsync(a->pad, 0, sizeof(double) * a->nreal, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(a->pad, 0, a->rsz * a->nreal, s);
   if (e != cudaSuccess) return apm_cuda(a, e, "apm kappa upload");
-  k_apm_pad<<<blocks_for(npx, 256), 256, 0, s>>>(a->g_re, n, F, a->pad);
-  int st = apm_fft(a, api.exec_d2z(a->fwd, a->pad, (cufftDoubleComplex*)a->spec), "kappa FFT");
+  k_apm_pad<T><<<blocks_for(npx, 256), 256, 0, s>>>(a->g_re, n, F, (T*)a->pad);
+  int st = fwd_fft(a, a->pad, a->spec);
   if (st) return st;
   // Map_fft_from_kappa (:183-197): fftconvolve(kappa, U, 'same') * fieldsize^2 / npix^2;
   // the inverse transform is unnormalised (1 / F^2)
   const double scale = a->fieldsize * a->fieldsize / ((double)n * n) / ((double)F * F);
   for (int t = 0; t < a->n_theta; ++t) {
-    k_apm_mul<<<blocks_for((long)a->ncplx, 256), 256, 0, s>>>(a->spec, a->uspec + (size_t)t * a->ncplx,
-                                                             (long)a->ncplx, a->work);
-    st = apm_fft(a, api.exec_z2d(a->inv, (cufftDoubleComplex*)a->work, a->pad + a->nreal), "kappa inverse FFT");
+    k_apm_mul<C><<<blocks_for((long)a->ncplx, 256), 256, 0, s>>>((const C*)a->spec, (const C*)a->Cx(a->uspec, t),
+                                                                (long)a->ncplx, (C*)a->work);
+    st = inv_fft(a, a->work, a->R(a->pad, 1));
     if (st) return st;
-    k_apm_crop_scaled<<<blocks_for(npx, 256), 256, 0, s>>>(a->pad + a->nreal, n, F, scale, a->maps + (size_t)t * npx);
+    k_apm_crop_scaled<T><<<blocks_for(npx, 256), 256, 0, s>>>((const T*)a->R(a->pad, 1), n, F, scale,
+                                                              a->maps + (size_t)t * npx);
   }
-  e = cudaGetLastError();
-  if (e == cudaSuccess && maps) e = cudaMemcpyAsync(maps, a->maps, sizeof(double) * npx * a->n_theta,
-                                                    cudaMemcpyDeviceToHost, s);
+  return apm_cuda(a, cudaGetLastError(), "apm kappa maps");
+}
+
+extern "C" int tp_apm_maps_from_kappa(tp_apm* a, const double* kappa, double* maps) {
+  TpRange nvtx_range("tp_apm_maps_from_kappa");
+  if (!a || !kappa) return TP_ERR_ARG;
+  cudaSetDevice(a->ctx->device);
+  int st = a->precision == TP_FP64 ? apm_kappa_t<double, double2>(a, kappa) : apm_kappa_t<float, float2>(a, kappa);
+  if (st) return st;
+  cudaStream_t s = a->ctx->stream;
+  cudaError_t e = cudaSuccess;
+  if (maps)
+    e = cudaMemcpyAsync(maps, a->maps, sizeof(double) * a->npix * a->npix * a->n_theta, cudaMemcpyDeviceToHost, s);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);
   return apm_cuda(a, e, "apm kappa maps");
 }
