@@ -92,6 +92,10 @@ def test_gpu_matches_oracle_other_sizes():
         ref = A.extract_map3(x, y, g, n, th, fs)
         got = G.extract_Map3(x, y, g, n, th, fs, ctx=ctx)
         assert rel(got, ref) < 1e-10
+        # six apertures: the general triplet reduction (five or fewer keep
+        # their sums in registers)
+        th6 = [1.0, 1.4, 1.7, 2.1, 2.5, 3.2]
+        assert rel(G.extract_Map3(x, y, g, n, th6, fs, ctx=ctx), A.extract_map3(x, y, g, n, th6, fs)) < 1e-10
         grid, w = A.cic_grid(x, y, g, n, fs)
         ac = G.aperture_mass_computer(n, 2.5, fs, ctx=ctx)
         m, xm = ac.Map_fft(grid, norm=w, return_mcross=True)

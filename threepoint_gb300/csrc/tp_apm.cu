@@ -297,6 +297,53 @@ __global__ void k_apm_map3(const double* __restrict__ maps, int npix, int n_thet
     if (s[q] != 0.0) atomicAdd(&sums[q], s[q]);
 }
 
+// The same sums for n_theta = NTH <= 5 apertures (up to 35 triplets): every
+// thread keeps its triplets' partial sums in registers over its grid-stride
+// pixels (one FP64 multiply per aperture pair and one FMA per triplet and
+// pixel) and reduces them once at the end, instead of a warp reduction per
+// triplet and pixel: about a fifth of the FP64 operations.
+template <int NTH>
+__global__ void k_apm_map3_reg(const double* __restrict__ maps, int npix, const int* __restrict__ cut, double* sums) {
+  constexpr int NT3 = NTH * (NTH + 1) * (NTH + 2) / 6;
+  __shared__ double s[NT3];
+  for (int q = threadIdx.x; q < NT3; q += blockDim.x) s[q] = 0.0;
+  int cutv[NTH];
+#pragma unroll
+  for (int a = 0; a < NTH; ++a) cutv[a] = cut[a];
+  __syncthreads();
+  double acc[NT3];
+#pragma unroll
+  for (int q = 0; q < NT3; ++q) acc[q] = 0.0;
+  const long npx = (long)npix * npix;
+  const long stride = (long)gridDim.x * blockDim.x;
+  for (long p = (long)blockIdx.x * blockDim.x + threadIdx.x; p < npx; p += stride) {
+    const int i = (int)(p / npix), j = (int)(p % npix);
+    const int edge = min(min(i, j), min(npix - 1 - i, npix - 1 - j));
+    double m[NTH];
+#pragma unroll
+    for (int a = 0; a < NTH; ++a) m[a] = maps[(size_t)a * npx + p];
+    int q = 0;
+#pragma unroll
+    for (int a = 0; a < NTH; ++a)
+#pragma unroll
+      for (int b = a; b < NTH; ++b) {
+        const double pab = m[a] * m[b];
+#pragma unroll
+        for (int c = b; c < NTH; ++c, ++q)
+          if (edge >= cutv[c]) acc[q] = fma(pab, m[c], acc[q]);
+      }
+  }
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int q = 0; q < NT3; ++q) {
+    double v = acc[q];
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (lane == 0) atomicAdd(&s[q], v);
+  }
+  __syncthreads();
+  for (int q = threadIdx.x; q < NT3; q += blockDim.x) atomicAdd(&sums[q], s[q]);
+}
+
 __global__ void k_apm_means(const double* sums, const double* counts, int ntrip, double* out) {
   const int q = blockIdx.x * blockDim.x + threadIdx.x;
   if (q < ntrip) out[q] = sums[q] / counts[q];
@@ -460,7 +507,15 @@ int apm_map3_device(tp_apm* a, int same_fieldsize) {
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   const long npx = (long)a->npix * a->npix;
   unsigned grid = (unsigned)std::min<long>(blocks_for(npx, 256), (long)sms * 8);
-  k_apm_map3<<<grid, 256, 0, s>>>(a->maps, a->npix, a->n_theta, same_fieldsize ? a->cut_same : a->cut, a->sums);
+  const int* cut = same_fieldsize ? a->cut_same : a->cut;
+  switch (a->n_theta) {
+    case 1: k_apm_map3_reg<1><<<grid, 256, 0, s>>>(a->maps, a->npix, cut, a->sums); break;
+    case 2: k_apm_map3_reg<2><<<grid, 256, 0, s>>>(a->maps, a->npix, cut, a->sums); break;
+    case 3: k_apm_map3_reg<3><<<grid, 256, 0, s>>>(a->maps, a->npix, cut, a->sums); break;
+    case 4: k_apm_map3_reg<4><<<grid, 256, 0, s>>>(a->maps, a->npix, cut, a->sums); break;
+    case 5: k_apm_map3_reg<5><<<grid, 256, 0, s>>>(a->maps, a->npix, cut, a->sums); break;
+    default: k_apm_map3<<<grid, 256, 0, s>>>(a->maps, a->npix, a->n_theta, cut, a->sums);
+  }
   e = cudaGetLastError();
   if (e != cudaSuccess) return apm_cuda(a, e, "apm map3 launch");
   // pixel counts of the windows are known on the host
