@@ -216,25 +216,58 @@ __global__ void __launch_bounds__(GEMM_NT, 1) k_gemm_tc(GemmArgs g) {
   tc_fence_after();
 
   if (ok && nslab > 0) {
-    const int row = m0 + warp * 32 + lane;
+    const int row0 = m0 + warp * 32;  // this warp's 32 rows; lane = row in the accumulator
+    const int row = row0 + lane;
     const uint32_t tw = tmem + ((uint32_t)(warp * 32) << 16);
     float dot = 0.f;
     const int f = g.flags;
+    // Row-major operands and results go through a per-warp 32 x 33 shared
+    // tile (the slab buffers are free once the last MMA has completed), so
+    // that global loads and stores move whole rows (32 consecutive columns per
+    // instruction) instead of one element per lane and row.
+    float* tile = reinterpret_cast<float*>(sb[0]) + warp * 32 * 33;
     for (int c0 = 0; c0 < N; c0 += 32) {
       float v[32];
       tc_ld32(tw + (uint32_t)c0, v);
-#pragma unroll 4
+      float zin[32];
+      if (f & EPI_DSILU) {
+        for (int r = 0; r < 32; ++r) tile[r * 33 + lane] = g.zin[(size_t)(row0 + r) * g.ldzin + c0 + lane];
+        __syncwarp();
+#pragma unroll
+        for (int j = 0; j < 32; ++j) zin[j] = tile[lane * 33 + j];
+        __syncwarp();
+      }
+      float zv[32], hv[32];
+#pragma unroll
       for (int j = 0; j < 32; ++j) {
         const int col = c0 + j;
         float z = v[j];
         if (f & EPI_BIAS) z += g.bias[col];
-        if (f & EPI_DSILU) z *= silu_grad_f(g.zin[(size_t)row * g.ldzin + col]);
-        if (f & EPI_STORE_Z) g.zout[(size_t)row * g.ldz + col] = z;
+        if (f & EPI_DSILU) z *= silu_grad_f(zin[j]);
+        zv[j] = z;
         const float hval = (f & EPI_SILU) ? silu_f(z) : z;
-        if (f & EPI_STORE_F32) g.out[(size_t)blockIdx.y * g.split_stride + (size_t)row * g.ldo + col] = hval;
-        if (f & EPI_STORE_H) g.h[(size_t)row * g.ldh + col] = __float2bfloat16_rn(hval);
+        hv[j] = hval;
         if (f & EPI_STORE_HT) g.ht[(size_t)col * g.ldht + row] = __float2bfloat16_rn(hval);
         if (f & EPI_DOT) dot = fmaf(hval, g.w5[col], dot);
+      }
+      if (f & EPI_STORE_Z) {
+#pragma unroll
+        for (int j = 0; j < 32; ++j) tile[lane * 33 + j] = zv[j];
+        __syncwarp();
+        for (int r = 0; r < 32; ++r) g.zout[(size_t)(row0 + r) * g.ldz + c0 + lane] = tile[r * 33 + lane];
+        __syncwarp();
+      }
+      if (f & (EPI_STORE_F32 | EPI_STORE_H)) {
+#pragma unroll
+        for (int j = 0; j < 32; ++j) tile[lane * 33 + j] = hv[j];
+        __syncwarp();
+        for (int r = 0; r < 32; ++r) {
+          const float x = tile[r * 33 + lane];
+          if (f & EPI_STORE_F32)
+            g.out[(size_t)blockIdx.y * g.split_stride + (size_t)(row0 + r) * g.ldo + c0 + lane] = x;
+          if (f & EPI_STORE_H) g.h[(size_t)(row0 + r) * g.ldh + c0 + lane] = __float2bfloat16_rn(x);
+        }
+        __syncwarp();
       }
     }
     if (f & EPI_DOT) g.y[row] = dot + *g.b5;
