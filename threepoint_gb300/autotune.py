@@ -6,7 +6,8 @@ registers per thread, 3 -> 80, 2 -> 128), TP_MAP3_UNROLL (node pairs per loop
 iteration), TP_MAP3_DUP_IN_LOOP (triangle pairs held in registers or formed
 at use) and TP_MAP3_PLT_GLOBAL (linear-P(k) table in shared memory or read
 through L1; the latter is what lets four CTAs fit an SM). The tuner builds the library for every candidate, times the kernel on
-a fixed batch (16 seeded cosmologies x 220 aperture-radius triplets, FP32,
+a fixed batch (64 seeded cosmologies x 220 aperture-radius triplets, the
+benchmark step's size, FP32,
 device-resident, CUDA events, best of 3 launches after a warm-up), writes the
 fastest to threepoint_gb300/tuned.json and rebuilds with it. build() passes
 tuned.json's values as -D flags.
@@ -31,7 +32,7 @@ ARCMIN = 2.9088820866e-4
 KNOBS = {"TP_MAP3_MINB": (3, 2), "TP_MAP3_UNROLL": (1, 2), "TP_MAP3_DUP_IN_LOOP": (1, 0), "TP_MAP3_PLT_GLOBAL": (0,)}
 
 
-def _workload(n_cosmo=16, seed=20261203):
+def _workload(n_cosmo=64, seed=20261203):
     rng = np.random.default_rng(seed)
     u = (rng.permutation(n_cosmo)[:, None] + rng.uniform(size=(n_cosmo, 5))) / n_cosmo
     lo = np.array([0.2, 0.7, 0.6, -1.2, 0.92])
@@ -98,7 +99,7 @@ def sweep(device=0, knobs=None):
 
     doc = {"k_map3": best["config"],
            "measured": {"device": torch.cuda.get_device_name(device), "date": time.strftime("%Y-%m-%d"),
-                        "workload": "16 seeded LHS cosmologies x 220 triplets, FP32, best of 3 launches",
+                        "workload": "64 seeded LHS cosmologies x 220 triplets, FP32, best of 3 launches",
                         "candidates": results},
            "command": "python -m threepoint_gb300.autotune"}
     with open(TUNED, "w") as f:
