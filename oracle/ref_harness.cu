@@ -7,8 +7,15 @@
 // GQ96_of_Pk, interpolation helpers) and its vendored hcubature_v. The table
 // loop below mirrors set_cosmology (cuda_version/bispectrum.cu:148-212) minus
 // the constant-memory uploads, which need a GPU.
+//
+// It also exposes the host side of the halo model (cuda_version/halomodel.cu):
+// sigma2(m) and dSigma2dm(m) (:179-277, the 128-entry mass tables that
+// setSigma2 / setdSigma2dm fill) and the __host__ __device__ functions hmf,
+// SiCi, r_200, u_NFW, concentration, get_sigma2, get_dSigma2dm and halo_bias
+// evaluated on the host after ref_halo_tables has filled the host arrays.
 #include "bispectrum.cuh"
 #include "cubature.h"
+#include "halomodel.cuh"
 
 #include <cstring>
 
@@ -24,6 +31,10 @@ double linear_pk(double k);
 double g_interpolated(int idx, double didx);
 double f_K_interpolated(int idx, double didx);
 void compute_coefficients(int idx, double didx, double* D1, double* r_sigma, double* n_eff, double* ncur);
+
+// halomodel.cu's device code reads this survey-variance table, which
+// apertureStatisticsCovariance.cu defines; that file is not compiled here.
+__constant__ double dev_sigma2_from_windowfunction_array[n_redshift_bins];
 
 extern "C" {
 
@@ -103,4 +114,27 @@ int ref_hcubature_v(unsigned fdim, integrand_v f, void* fdata, unsigned dim, con
   return hcubature_v(fdim, f, fdata, dim, xmin, xmax, maxEval, reqAbsError, reqRelError, (error_norm)norm, val,
                      err);
 }
+
+// setSigma2 / setdSigma2dm (halomodel.cu:197-214,262-276) without the
+// constant-memory uploads: out[0..127] = sigma2(m_i), out[128..255] =
+// dSigma2dm(m_i), m_i = 10^(logMmin + i (logMmax - logMmin) / n_mbins); the
+// host arrays that get_sigma2 / get_dSigma2dm read are filled too
+void ref_halo_tables(double* out) {
+  const double deltaM = (logMmax - logMmin) / n_mbins;
+  for (int i = 0; i < n_mbins; i++) {
+    const double m = pow(10, logMmin + i * deltaM);
+    sigma2_array[i] = sigma2(m);
+    dSigma2dm_array[i] = dSigma2dm(m);
+    out[i] = sigma2_array[i];
+    out[n_mbins + i] = dSigma2dm_array[i];
+  }
+}
+double ref_hmf(double m, double z) { return hmf(m, z); }
+void ref_SiCi(double x, double* si, double* ci) { SiCi(x, *si, *ci); }
+double ref_r_200(double m, double z) { return r_200(m, z); }
+double ref_u_NFW(double k, double m, double z) { return u_NFW(k, m, z); }
+double ref_concentration(double m, double z) { return concentration(m, z); }
+double ref_get_sigma2(double m, double z) { return get_sigma2(m, z); }
+double ref_get_dSigma2dm(double m, double z) { return get_dSigma2dm(m, z); }
+double ref_halo_bias(double m, double z) { return halo_bias(m, z); }
 }
