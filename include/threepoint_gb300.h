@@ -328,21 +328,49 @@ int tp_apm_extract_map3_device(tp_apm* apm, const double* x_device, const double
 int tp_ogata_weights(double* out);
 
 /* Covariance terms of <Map^3> (cuda_version/apertureStatisticsCovariance.cu):
- * T1_total, T2_total, T4_total (:272-683) for pairs of triplets.
- * term: 1, 2 or 4; geometry TP_GEOM_*; theta_max [rad] and area [rad^2] as in
- * covarianceParameters (cosmology.cu:92-170). out[i] = T_term(th123[i], th456[i]). */
+ * T1_total, T2_total, T4_total (:272-683) and the halo-model terms
+ * T5_total, T6_total, T7_total (:685-1044) for pairs of triplets.
+ * term: 1, 2, 4, 5, 6 or 7; geometry TP_GEOM_*; theta_max [rad] and area
+ * [rad^2] as in covarianceParameters (cosmology.cu:92-170).
+ * out[i] = T_term(th123[i], th456[i]). T5 and T7 exist for the infinite
+ * geometry only, T6 for the square and the rectangle (0 for the infinite
+ * geometry, as T6_total returns); the others are TP_ERR_ARG, where the
+ * reference throws. T5-T7 are evaluated in FP64 whatever precision asks. */
 int tp_cov_total_batch(tp_ctx* ctx, int cosmo_index, int term, int geometry, double theta_max, double area,
                        const double* th123, const double* th456, int n, int precision, double* out,
                        int* n_capped);
 
-/* Single covariance terms T1(th1..th6), T2(th1..th6), T4(th1..th6)
- * (apertureStatisticsCovariance.cu:1065-1197) for n six-tuples th6[n][6],
+/* Single covariance terms T1, T2, T4, T5, T6, T7 of (th1..th6)
+ * (apertureStatisticsCovariance.cu:1065-1313) for n six-tuples th6[n][6],
  * without the permutation sums. T2 is 0 for the infinite geometry; T4 exists
  * only for the infinite geometry (normalised by area), as in the reference,
  * whose T4 throws for the others (TP_ERR_ARG here). *n_capped (optional)
  * receives the number of integrals that hit a cap. */
 int tp_cov_term_batch(tp_ctx* ctx, int cosmo_index, int term, int geometry, double theta_max, double area,
                       const double* th6, int n, int precision, double* out, int* n_capped);
+
+/* Relative tolerance of the T5 / T6 / T7 integrals (term 5..7); 0 restores
+ * the reference's 1e-2 / 1e-1 / 1e-1 (apertureStatisticsCovariance.cu:1222,
+ * 1271, 1307). */
+int tp_ctx_set_cov_tolerance(tp_ctx* ctx, int term, double rel_tol);
+
+/* Halo model of T5-T7 (cuda_version/halomodel.cu), built per cosmology on
+ * first use.
+ * tp_halo_tables: out[0..127] = sigma^2(m_i), out[128..255] = dsigma^2/dm(m_i)
+ *   at z = 0, m_i = 10^(9 + i/16) Msun/h (setSigma2 / setdSigma2dm, :197-276).
+ * tp_halo_los: at rows pts[n][7] = (m, l1, ..., l6), m in [1e9, 1e17]:
+ *   tri[i] = trispectrum_limber_integrated(0, z_max, m, l1..l4) and
+ *   penta[i] = pentaspectrum_limber_integrated(0, z_max, m, l1..l6) (:430-510).
+ * tp_halo_integrand_points: the integrand of T5 (x rows of 6: ln l1, ln l2,
+ *   ln l5, phi1, phi2, m), T6 (rows of 7: ln l3, ln l4, ln l5, phi3, phi4,
+ *   phi5, m; geometry square or rectangle) or T7 (rows of 7: ln l1, ln l2,
+ *   ln l4, ln l5, phi1, phi2, m) for the radii th6 (integrand_T5_infinite,
+ *   integrand_T6_square / _rectangle, integrand_T7_infinite, :2151-2314),
+ *   before the 1/area/(2 pi)^n factors. */
+int tp_halo_tables(tp_ctx* ctx, int cosmo_index, double* out);
+int tp_halo_los(tp_ctx* ctx, int cosmo_index, const double* pts, long n, double* tri, double* penta);
+int tp_halo_integrand_points(tp_ctx* ctx, int cosmo_index, int term, int geometry, double theta_max,
+                             const double* th6, const double* x, long n, double* out);
 
 /* ---- likelihood of <Map^3> model vectors -------------------------------- */
 

@@ -102,6 +102,27 @@ def lib():
             getattr(L, n).argtypes = [p, cp, dp, dp]
         L.orc_G_square.restype = d
         L.orc_G_square.argtypes = [d, d, d]
+        L.orc_halo_tables.argtypes = [p, dp]
+        L.orc_halo_ctx_create.restype = p
+        L.orc_halo_ctx_create.argtypes = [p, cp, i, dp]
+        L.orc_halo_ctx_destroy.argtypes = [p]
+        L.orc_halo_ctx_lmax.restype = d
+        L.orc_halo_ctx_lmax.argtypes = [p]
+        for n, k in (("orc_hmf", 2), ("orc_u_nfw", 3), ("orc_get_sigma2", 2), ("orc_get_dsigma2", 2),
+                     ("orc_r_200", 1)):
+            getattr(L, n).restype = d
+            getattr(L, n).argtypes = [p] + [d] * k
+        L.orc_concentration.restype = d
+        L.orc_concentration.argtypes = [d, d]
+        L.orc_sici.argtypes = [d, dp, dp]
+        L.orc_halo_los.argtypes = [p, dp, l, dp, dp]
+        L.orc_halo_integrand.argtypes = [p, cp, i, dp, d, dp, l, dp]
+        L.orc_T_halo.restype = d
+        L.orc_T_halo.argtypes = [p, cp, i, dp, d, l, dp, C.POINTER(l)]
+        L.orc_halo_total_terms.restype = i
+        L.orc_halo_total_terms.argtypes = [i, dp, dp, C.POINTER(i), C.POINTER(i)]
+        L.orc_T_halo_total.restype = d
+        L.orc_T_halo_total.argtypes = [p, cp, i, dp, dp, d, l]
         L.orc_set_threads.argtypes = [i]
         _lib = L
     return _lib
@@ -273,11 +294,63 @@ class Tables:
             return L.orc_T2(self._h, C.byref(params), _dp(th)), 0
         return L.orc_T4(self._h, C.byref(params), _dp(th), rel, C.byref(nev)), nev.value
 
+    # ---- halo model (T5, T6, T7) ----
+    def halo_tables(self):
+        """sigma^2(m_i) and dsigma^2/dm(m_i) at z = 0, 128 masses each."""
+        out = np.zeros(256)
+        lib().orc_halo_tables(self._h, _dp(out))
+        return out[:128].copy(), out[128:].copy()
+
+    def halo_los(self, pts):
+        """Line-of-sight one-halo trispectrum (l1..l4) and pentaspectrum
+        (l1..l6) at rows (m, l1, ..., l6)."""
+        pts = np.ascontiguousarray(pts, dtype=np.float64).reshape(-1, 7)
+        tri, pen = np.zeros(len(pts)), np.zeros(len(pts))
+        lib().orc_halo_los(self._h, _dp(pts), len(pts), _dp(tri), _dp(pen))
+        return tri, pen
+
+    def halo_integrand(self, term, params: CovParams, th6, lmax, x):
+        ndim = 6 if term == 5 else 7
+        x = np.ascontiguousarray(x, dtype=np.float64).reshape(-1, ndim)
+        th = np.array(th6, dtype=np.float64)
+        out = np.zeros(len(x))
+        lib().orc_halo_integrand(self._h, C.byref(params), term, _dp(th), lmax, _dp(x), len(x), _dp(out))
+        return out
+
+    def cov_T_halo(self, term, params: CovParams, th6, rel=0.0, max_eval=0):
+        """T5/T6/T7 single term: (value, error estimate, evaluations)."""
+        th = np.array(th6, dtype=np.float64)
+        err, nev = C.c_double(0), C.c_long(0)
+        v = lib().orc_T_halo(self._h, C.byref(params), term, _dp(th), rel, max_eval, C.byref(err), C.byref(nev))
+        return v, err.value, nev.value
+
+    def cov_total_halo(self, term, params: CovParams, th123, th456, rel=0.0, max_eval=0):
+        a = np.array(th123, dtype=np.float64)
+        b = np.array(th456, dtype=np.float64)
+        return lib().orc_T_halo_total(self._h, C.byref(params), term, _dp(a), _dp(b), rel, max_eval)
+
     def cov_total(self, term, params: CovParams, th123, th456):
         a = np.array(th123, dtype=np.float64)
         b = np.array(th456, dtype=np.float64)
         fn = {1: lib().orc_T1_total, 2: lib().orc_T2_total, 4: lib().orc_T4_total}[term]
         return fn(self._h, C.byref(params), _dp(a), _dp(b))
+
+
+def halo_total_terms(term, th123, th456):
+    """(multiplicity, argument indices into (a0, a1, a2, b0, b1, b2)) of the
+    reference's T5_total / T6_total / T7_total."""
+    a = np.array(th123, dtype=np.float64)
+    b = np.array(th456, dtype=np.float64)
+    mult = (C.c_int * 16)()
+    idx = (C.c_int * 96)()
+    n = lib().orc_halo_total_terms(term, _dp(a), _dp(b), mult, idx)
+    return [(mult[k], tuple(idx[6 * k:6 * k + 6])) for k in range(n)]
+
+
+def sici(x):
+    si, ci = C.c_double(0), C.c_double(0)
+    lib().orc_sici(x, C.byref(si), C.byref(ci))
+    return si.value, ci.value
 
 
 def ogata_weights():
@@ -334,5 +407,12 @@ def ref_lib():
         L.ref_gq96.argtypes = [dp, dp]
         L.ref_hcubature_v.restype = i
         L.ref_hcubature_v.argtypes = [C.c_uint, p, p, C.c_uint, dp, dp, C.c_size_t, d, d, i, dp, dp]
+        if hasattr(L, "ref_halo_tables"):
+            L.ref_halo_tables.argtypes = [dp]
+            for n, k in (("ref_hmf", 2), ("ref_r_200", 2), ("ref_u_NFW", 3), ("ref_concentration", 2),
+                         ("ref_get_sigma2", 2), ("ref_get_dSigma2dm", 2), ("ref_halo_bias", 2)):
+                getattr(L, n).restype = d
+                getattr(L, n).argtypes = [d] * k
+            L.ref_SiCi.argtypes = [d, dp, dp]
         _ref = L
     return _ref

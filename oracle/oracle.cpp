@@ -10,6 +10,7 @@
 #include "oracle.hpp"
 
 #include <algorithm>
+#include <array>
 #include <cfloat>
 #include <cmath>
 #include <complex>
@@ -86,6 +87,9 @@ struct orc_tables {
   double sigma = 0, ngal = 1;
   bool constant_ps = false;
   bool analytic = false;
+  // halo model mass tables (sigma^2(m), dsigma^2/dm at z = 0), built on first use
+  bool halo = false;
+  double sig2[128], dsig2[128];
 };
 
 namespace {
@@ -1627,6 +1631,511 @@ extern "C" double orc_T4_total(const orc_tables* t, const orc_cov_params* p, con
     r = T(t3, t0, t1, t2, t4, t5) + T(t3, t0, t2, t1, t4, t5) + T(t3, t1, t2, t0, t4, t4) + 2 * T(t4, t0, t1, t2, t3, t4) + 2 * T(t4, t1, t2, t0, t3, t4) + 2 * T(t4, t0, t2, t1, t3, t4);
   } else {
     r = T(t3, t0, t1, t2, t4, t5) + T(t3, t0, t2, t1, t4, t5) + T(t3, t1, t2, t0, t4, t5) + T(t4, t0, t1, t2, t3, t5) + T(t4, t0, t2, t1, t3, t5) + T(t4, t1, t2, t0, t3, t5) + T(t5, t0, t1, t2, t3, t4) + T(t5, t0, t2, t1, t3, t4) + T(t5, t1, t2, t0, t3, t4);
+  }
+  return r;
+}
+
+// ===========================================================================
+// Halo model (cuda_version/halomodel.cu) and the covariance terms built on
+// it: T5, T6, T7 (apertureStatisticsCovariance.cu:685-1063,1199-1313,2151-2314)
+// ===========================================================================
+namespace {
+
+constexpr int NM = 128;                          // n_mbins, halomodel.cuh:17
+constexpr double LOGMMIN = 9, LOGMMAX = 17;      // halomodel.cuh:15-16
+constexpr double RHO_CRIT = 2.7754e11;           // [Msun h^2 / Mpc^3], halomodel.cu:54
+
+// sigma^2(m) at z = 0: top-hat variance of radius R(m), adaptive 1-D
+// integral over k in [0, 1e12] at relative 1e-4 (halomodel.cu:179-220)
+struct SigmaCtx {
+  const orc_tables* t;
+  double R, dR;
+  int deriv;
+};
+int integrand_sigma_v(unsigned ndim, size_t npts, const double* k, void* fdata, unsigned, double* fval) {
+  const SigmaCtx* c = (const SigmaCtx*)fdata;
+  for (size_t i = 0; i < npts; ++i) {
+    double k_ = k[i * ndim];
+    double W = window(k_ * c->R, 0);
+    if (c->deriv)
+      fval[i] = k_ * k_ * W * window(k_ * c->R, 4) * c->dR * linear_pk(c->t, k_) * k_;
+    else
+      fval[i] = k_ * k_ * W * W * linear_pk(c->t, k_);
+  }
+  return 0;
+}
+
+// setSigma2 / setdSigma2dm (halomodel.cu:197-214,262-276): masses
+// m_i = 10^(logMmin + i (logMmax - logMmin) / n_mbins). The host linear_pk
+// the reference calls there is always Eisenstein & Hu (its Pk_given global is
+// never set; see orc_tables_create), so a given P(k) table is ignored here.
+void ensure_halo(const orc_tables* tc) {
+  orc_tables* t = const_cast<orc_tables*>(tc);
+  if (t->halo) return;
+  const bool given = t->pk_given;
+  t->pk_given = false;
+  const double rhobar = RHO_CRIT * t->c.om;
+  const double deltaM = (LOGMMAX - LOGMMIN) / NM;
+  for (int i = 0; i < NM; ++i) {
+    double m = pow(10, LOGMMIN + i * deltaM);
+    SigmaCtx c{t, pow(0.75 / PI * m / rhobar, 1. / 3.), 0, 0};
+    double kmin[1] = {0}, kmax[1] = {1e12}, r, e;
+    orc_hcubature_v(1, integrand_sigma_v, &c, 1, kmin, kmax, 0, 0, 1e-4, ORC_ERROR_L1, &r, &e);
+    t->sig2[i] = r / 2 / PI / PI;
+    c.dR = pow(0.75 / PI / rhobar, 1. / 3.) * pow(m, -2. / 3.) / 3.;
+    c.deriv = 1;
+    orc_hcubature_v(1, integrand_sigma_v, &c, 1, kmin, kmax, 0, 0, 1e-4, ORC_ERROR_L1, &r, &e);
+    t->dsig2[i] = r / PI / PI;
+  }
+  t->pk_given = given;
+  t->halo = true;
+}
+
+// linear interpolation in a z-table on the grid z_i = i z_max / (n - 1), as
+// the halo-model code reads the tables (halomodel.cu:300-311,398-408), which
+// set_cosmology fills at the bin centres (i + 0.5) z_max / n
+double halo_zinterp(const orc_tables* t, const double* arr, double z) {
+  double didx = z / t->z_max * (NZ - 1);
+  int idx = (int)didx;
+  didx = didx - idx;
+  if (idx == NZ - 1) {
+    idx = NZ - 2;
+    didx = 1.;
+  }
+  return arr[idx] * (1 - didx) + arr[idx + 1] * didx;
+}
+
+// mass-table lookup, halomodel.cu:279-299: the index runs over n_mbins - 1
+// intervals of [logMmin, logMmax] (the table was filled with n_mbins)
+double halo_minterp(const double* arr, double m) {
+  double didx = (log10(m) - LOGMMIN) / (LOGMMAX - LOGMMIN) * (NM - 1);
+  int idx = (int)didx;
+  didx = didx - idx;
+  if (idx == NM - 1) {
+    idx = NM - 2;
+    didx = 1.;
+  }
+  return arr[idx] * (1 - didx) + arr[idx + 1] * didx;
+}
+
+// get_sigma2 / get_dSigma2dm, halomodel.cu:279-375
+double get_sigma2(const orc_tables* t, double m, double z) {
+  double D1 = halo_zinterp(t, t->D1, z);
+  return halo_minterp(t->sig2, m) * D1 * D1;
+}
+double get_dsigma2(const orc_tables* t, double m, double z) {
+  double D1 = halo_zinterp(t, t->D1, z);
+  return halo_minterp(t->dsig2, m) * D1 * D1;
+}
+
+// Sheth-Tormen mass function dn/dm, halomodel.cu:31-59
+double hmf(const orc_tables* t, double m, double z) {
+  const double A = 0.322, q = 0.707, p = 0.3;
+  double sigma2 = get_sigma2(t, m, z);
+  double dsigma2 = get_dsigma2(t, m, z);
+  double deltac = 1.686 * (1 + 0.0123 * log10(om_m_of_z(t, z)));
+  double rho_mean = RHO_CRIT * t->c.om;
+  double nu = deltac * deltac / sigma2;
+  return -rho_mean / m / sigma2 * dsigma2 * A * (1 + pow(q * nu, -p)) * sqrt(q * nu / 2 / PI) * exp(-0.5 * q * nu);
+}
+
+// Sine and cosine integrals Si(x), Ci(x) by the rational approximations the
+// reference uses (halomodel.cu:61-105; the Pade approximants of Rowe et al.
+// 2015, GalSim, Appendix B: x < 4 a ratio of even polynomials, x >= 4 the
+// auxiliary functions f, g in 1/x^2)
+void sici(double x, double& si, double& ci) {
+  double x2 = x * x, x4 = x2 * x2, x6 = x2 * x4, x8 = x4 * x4, x10 = x8 * x2, x12 = x6 * x6, x14 = x12 * x2;
+  if (x < 4) {
+    double a = 1 - 4.54393409816329991e-2 * x2 + 1.15457225751016682e-3 * x4 - 1.41018536821330254e-5 * x6 +
+               9.43280809438713025e-8 * x8 - 3.53201978997168357e-10 * x10 + 7.08240282274875911e-13 * x12 -
+               6.05338212010422477e-16 * x14;
+    double b = 1 + 1.01162145739225565e-2 * x2 + 4.99175116169755106e-5 * x4 + 1.55654986308745614e-7 * x6 +
+               3.28067571055789734e-10 * x8 + 4.5049097575386581e-13 * x10 + 3.21107051193712168e-16 * x12;
+    si = x * a / b;
+    a = -0.25 + 7.51851524438898291e-3 * x2 - 1.27528342240267686e-4 * x4 + 1.05297363846239184e-6 * x6 -
+        4.68889508144848019e-9 * x8 + 1.06480802891189243e-11 * x10 - 9.93728488857585407e-15 * x12;
+    b = 1 + 1.1592605689110735e-2 * x2 + 6.72126800814254432e-5 * x4 + 2.55533277086129636e-7 * x6 +
+        6.97071295760958946e-10 * x8 + 1.38536352772778619e-12 * x10 + 1.89106054713059759e-15 * x12 +
+        1.39759616731376855e-18 * x14;
+    ci = 0.5772156649 + std::log(x) + x2 * a / b;
+    return;
+  }
+  double x16 = x8 * x8, x18 = x16 * x2, x20 = x10 * x10;
+  double cx = cos(x), sx = sin(x);
+  double f = (1 + 7.44437068161936700618e2 / x2 + 1.96396372895146869801e5 / x4 + 2.37750310125431834034e7 / x6 +
+              1.43073403821274636888e9 / x8 + 4.33736238870432522765e10 / x10 + 6.40533830574022022911e11 / x12 +
+              4.20968180571076940208e12 / x14 + 1.00795182980368574617e13 / x16 + 4.94816688199951963482e12 / x18 -
+              4.94701168645415959931e11 / x20) /
+             (1 + 7.46437068161927678031e2 / x2 + 1.97865247031583951450e5 / x4 + 2.41535670165126845144e7 / x6 +
+              1.47478952192985464958e9 / x8 + 4.58595115847765779830e10 / x10 + 7.08501308149515401563e11 / x12 +
+              5.06084464593475076774e12 / x14 + 1.43468549171581016479e13 / x16 + 1.11535493509914254097e13 / x18) /
+             x;
+  double g = (1 + 8.1359520115168615e2 / x2 + 2.35239181626478200e5 / x4 + 3.12557570795778731e7 / x6 +
+              2.06297595146763354e9 / x8 + 6.83052205423625007e10 / x10 + 1.09049528450362786e12 / x12 +
+              7.57664583257834349e12 / x14 + 1.81004487464664575e13 / x16 + 6.43291613143049485e12 / x18 -
+              1.36517137670871689e12 / x20) /
+             (1 + 8.19595201151451564e2 / x2 + 2.40036752835578777e5 / x4 + 3.26026661647090822e7 / x6 +
+              2.23355543278099360e9 / x8 + 7.87465017341829930e10 / x10 + 1.39866710696414565e12 / x12 +
+              1.17164723371736605e13 / x14 + 4.01839087307656620e13 / x16 + 3.99653257887490811e13 / x18) /
+             x2;
+  si = 0.5 * PI - f * cx - g * sx;
+  ci = f * sx - g * cx;
+}
+
+// halomodel.cu:107-119 (r_200 [Mpc/h]), :142-152 (Duffy et al. 2008 concentration)
+double r_200(const orc_tables* t, double m) { return pow(0.75 / PI * m / (RHO_CRIT * t->c.om) / 200, 1. / 3.); }
+double concentration(double m, double z) { return 10.14 * pow(m / 2e12, -0.081) * pow(1 + z, -1.01); }
+
+// Fourier transform of the NFW profile truncated at r_200, halomodel.cu:121-140
+double u_nfw(const orc_tables* t, double k, double m, double z) {
+  double c = concentration(m, z);
+  double arg1 = k * r_200(t, m) / c;
+  double arg2 = arg1 * (1 + c);
+  double si1, ci1, si2, ci2;
+  sici(arg1, si1, ci1);
+  sici(arg2, si2, ci2);
+  double term1 = sin(arg1) * (si2 - si1);
+  double term2 = cos(arg1) * (ci2 - ci1);
+  double term3 = -sin(arg1 * c) / arg2;
+  double F = std::log(1. + c) - c / (1. + c);
+  return (term1 + term2 + term3) / F;
+}
+
+// one-halo convergence tri- and pentaspectrum integrands at (m, z) and their
+// 96-point Gauss-Legendre line-of-sight integrals (halomodel.cu:392-510)
+double trispectrum_integrand(const orc_tables* t, double m, double z, double l1, double l2, double l3, double l4) {
+  double g = halo_zinterp(t, t->g, z);
+  double chi = halo_zinterp(t, t->f_K, z);
+  double rhobar = RHO_CRIT * t->c.om;
+  double result = hmf(t, m, z) * g * g * g * g / chi / chi;
+  result *= C_OVER_H0 / E(t, z);
+  result *= u_nfw(t, l1 / chi, m, z) * u_nfw(t, l2 / chi, m, z) * u_nfw(t, l3 / chi, m, z) * u_nfw(t, l4 / chi, m, z);
+  result *= m * m * m * m / rhobar / rhobar / rhobar / rhobar;
+  result *= pow(1.5 * t->c.om / C_OVER_H0 / C_OVER_H0, 4);
+  result *= pow(1 + z, 4);
+  return result;
+}
+double trispectrum_los(const orc_tables* t, double m, double l1, double l2, double l3, double l4) {
+  const GQ96& G = gq96();
+  double cx = t->z_max / 2, dx = t->z_max / 2, q = 0;
+  for (int i = 0; i < 48; i++)
+    q += G.w[i] * (trispectrum_integrand(t, m, cx - dx * G.a[i], l1, l2, l3, l4) +
+                   trispectrum_integrand(t, m, cx + dx * G.a[i], l1, l2, l3, l4));
+  return q * dx;
+}
+double pentaspectrum_integrand(const orc_tables* t, double m, double z, const double* l) {
+  double g = halo_zinterp(t, t->g, z);
+  double chi = halo_zinterp(t, t->f_K, z);
+  double rhobar = RHO_CRIT * t->c.om;
+  double result = 1;
+  result *= pow(g, 6);
+  result /= pow(chi, 4);
+  result *= C_OVER_H0 / E(t, z);
+  result *= u_nfw(t, l[0] / chi, m, z) * u_nfw(t, l[1] / chi, m, z) * u_nfw(t, l[2] / chi, m, z);
+  result *= u_nfw(t, l[3] / chi, m, z) * u_nfw(t, l[4] / chi, m, z) * u_nfw(t, l[5] / chi, m, z);
+  result *= pow(m / rhobar, 6) * hmf(t, m, z);
+  result *= pow(1.5 * t->c.om / C_OVER_H0 / C_OVER_H0, 6);
+  result *= pow(1 + z, 6);
+  return result;
+}
+double pentaspectrum_los(const orc_tables* t, double m, const double* l) {
+  const GQ96& G = gq96();
+  double cx = t->z_max / 2, dx = t->z_max / 2, q = 0;
+  for (int i = 0; i < 48; i++)
+    q += G.w[i] * (pentaspectrum_integrand(t, m, cx - dx * G.a[i], l) + pentaspectrum_integrand(t, m, cx + dx * G.a[i], l));
+  return q * dx;
+}
+
+// integrand_T5_infinite, integrand_T6_square / _rectangle, integrand_T7_infinite
+// (apertureStatisticsCovariance.cu:2151-2314). The reference's device lower
+// bound dev_lMin is the driver's lMin = 0 (calculateApertureStatisticsCovariance.cu:89,
+// uploaded once by initCovariance), so only l <= 0 is cut; a squared length
+// that rounds below zero counts as zero length.
+struct HaloCtx {
+  const orc_tables* t;
+  const orc_cov_params* p;
+  double th[6];
+  double lMax;
+};
+int integrand_T5_v(unsigned ndim, size_t npts, const double* x, void* fdata, unsigned, double* fval) {
+  const HaloCtx* c = (const HaloCtx*)fdata;
+  const double* th = c->th;
+#pragma omp parallel for schedule(dynamic, 1) if (npts > 8)
+  for (long i = 0; i < (long)npts; ++i) {
+    const double* v = x + i * ndim;
+    double l1 = exp(v[0]), l2 = exp(v[1]), l5 = exp(v[2]), phi1 = v[3], phi2 = v[4], m = v[5];
+    double s3 = l1 * l1 + l2 * l2 + 2 * l1 * l2 * cos(phi1);
+    double s6 = l1 * l1 + l5 * l5 + 2 * l1 * l5 * cos(phi2);
+    double res = 0;
+    if (s3 > 0 && s6 > 0) {
+      double l3 = sqrt(s3), l6 = sqrt(s6), l4 = l1;
+      if (!(l3 > c->lMax || l6 > c->lMax)) {
+        res = uHat(l1 * th[0]) * uHat(l2 * th[1]) * uHat(l3 * th[2]) * uHat(l4 * th[3]) * uHat(l5 * th[4]) *
+              uHat(l6 * th[5]);
+        res *= Pell(c->t, l1);
+        res *= trispectrum_los(c->t, m, l2, l3, l5, l6);
+        res *= l1 * l2 * l5;
+        res *= l1 * l2 * l5;
+      }
+    }
+    fval[i] = res;
+  }
+  return 0;
+}
+int integrand_T6_v(unsigned ndim, size_t npts, const double* x, void* fdata, unsigned, double* fval) {
+  const HaloCtx* c = (const HaloCtx*)fdata;
+  const double* th = c->th;
+#pragma omp parallel for schedule(dynamic, 1) if (npts > 8)
+  for (long i = 0; i < (long)npts; ++i) {
+    const double* v = x + i * ndim;
+    double l3 = exp(v[0]), l4 = exp(v[1]), l5 = exp(v[2]), phi3 = v[3], phi4 = v[4], phi5 = v[5], m = v[6];
+    double l3x = l3 * cos(phi3), l3y = l3 * sin(phi3);
+    double l6 = l3 * l3 + l4 * l4 + l5 * l5 +
+                2 * (l3 * l4 * cos(phi3 - phi4) - l3 * l5 * cos(phi3 - phi5) - l4 * l5 * cos(phi4 - phi5));
+    l6 = l6 > 0 ? sqrt(l6) : 0;
+    double res = 0;
+    if (!(l6 <= 0 || l6 > c->lMax)) {
+      double G = G_rect(c->p->thetaMax, side_y(c->p), l3x, l3y);
+      res = uHat(l3 * th[2]) * uHat(l4 * th[3]) * uHat(l5 * th[4]) * uHat(l6 * th[5]);
+      res *= trispectrum_los(c->t, m, l3, l4, l5, l6);
+      res *= l3 * l4 * l5;
+      res *= l3 * l4 * l5;
+      res *= G;
+    }
+    fval[i] = res;
+  }
+  return 0;
+}
+int integrand_T7_v(unsigned ndim, size_t npts, const double* x, void* fdata, unsigned, double* fval) {
+  const HaloCtx* c = (const HaloCtx*)fdata;
+  const double* th = c->th;
+#pragma omp parallel for schedule(dynamic, 1) if (npts > 8)
+  for (long i = 0; i < (long)npts; ++i) {
+    const double* v = x + i * ndim;
+    double l1 = exp(v[0]), l2 = exp(v[1]), l4 = exp(v[2]), l5 = exp(v[3]), phi1 = v[4], phi2 = v[5], m = v[6];
+    double l3 = l1 * l1 + l2 * l2 + 2 * l1 * l2 * cos(phi1);
+    double l6 = l4 * l4 + l5 * l5 + 2 * l4 * l5 * cos(phi2);
+    double res = 0;
+    if (!(l3 <= 0 || l6 <= 0)) {
+      double l[6] = {l1, l2, sqrt(l3), l4, l5, sqrt(l6)};
+      res = uHat(l[0] * th[0]) * uHat(l[1] * th[1]) * uHat(l[2] * th[2]) * uHat(l[3] * th[3]) * uHat(l[4] * th[4]) *
+            uHat(l[5] * th[5]);
+      res *= pentaspectrum_los(c->t, m, l);
+      res *= l1 * l2 * l4 * l5;
+      res *= l1 * l2 * l4 * l5;
+    }
+    fval[i] = res;
+  }
+  return 0;
+}
+
+// host lower bound of T5/T6/T7 (the reference sets its host lMin to 1e-4 there)
+constexpr double HALO_LMIN = 1e-4;
+
+}  // namespace
+
+// the T5 / T6 / T7 integrand behind the cubature interface, for pinning the
+// cubature on these integrands to the reference's own hcubature_v
+struct orc_halo_ctx {
+  HaloCtx c;
+  orc_cov_params p;
+  int term;
+};
+extern "C" orc_halo_ctx* orc_halo_ctx_create(const orc_tables* t, const orc_cov_params* p, int term, const double* th) {
+  ensure_halo(t);
+  orc_halo_ctx* h = new orc_halo_ctx();
+  h->p = *p;
+  h->term = term;
+  double tmin123 = std::min({th[0], th[1], th[2]}), tmin456 = std::min({th[3], th[4], th[5]});
+  double lMax = 10. / (term == 7 ? std::min(tmin123, tmin456) : std::max(tmin123, tmin456));
+  h->c = HaloCtx{t, &h->p, {th[0], th[1], th[2], th[3], th[4], th[5]}, lMax};
+  return h;
+}
+extern "C" void orc_halo_ctx_destroy(orc_halo_ctx* h) { delete h; }
+extern "C" double orc_halo_ctx_lmax(const orc_halo_ctx* h) { return h->c.lMax; }
+extern "C" int orc_integrand_halo_v(unsigned ndim, size_t npts, const double* x, void* fdata, unsigned fdim,
+                                    double* fval) {
+  orc_halo_ctx* h = (orc_halo_ctx*)fdata;
+  if (h->term == 5) return integrand_T5_v(ndim, npts, x, &h->c, fdim, fval);
+  if (h->term == 6) return integrand_T6_v(ndim, npts, x, &h->c, fdim, fval);
+  return integrand_T7_v(ndim, npts, x, &h->c, fdim, fval);
+}
+
+extern "C" void orc_halo_tables(const orc_tables* t, double* out) {
+  ensure_halo(t);
+  std::memcpy(out, t->sig2, sizeof(double) * NM);
+  std::memcpy(out + NM, t->dsig2, sizeof(double) * NM);
+}
+extern "C" double orc_hmf(const orc_tables* t, double m, double z) {
+  ensure_halo(t);
+  return hmf(t, m, z);
+}
+extern "C" void orc_sici(double x, double* si, double* ci) { sici(x, *si, *ci); }
+extern "C" double orc_u_nfw(const orc_tables* t, double k, double m, double z) { return u_nfw(t, k, m, z); }
+extern "C" double orc_concentration(double m, double z) { return concentration(m, z); }
+extern "C" double orc_r_200(const orc_tables* t, double m) { return r_200(t, m); }
+extern "C" double orc_get_sigma2(const orc_tables* t, double m, double z) {
+  ensure_halo(t);
+  return get_sigma2(t, m, z);
+}
+extern "C" double orc_get_dsigma2(const orc_tables* t, double m, double z) {
+  ensure_halo(t);
+  return get_dsigma2(t, m, z);
+}
+// line-of-sight tri-/pentaspectrum at points: pts rows (m, l1..l6); the
+// trispectrum uses l1..l4
+extern "C" void orc_halo_los(const orc_tables* t, const double* pts, long n, double* tri, double* penta) {
+  ensure_halo(t);
+#pragma omp parallel for schedule(dynamic, 1)
+  for (long i = 0; i < n; ++i) {
+    const double* r = pts + 7 * i;
+    tri[i] = trispectrum_los(t, r[0], r[1], r[2], r[3], r[4]);
+    penta[i] = pentaspectrum_los(t, r[0], r + 1);
+  }
+}
+// integrand values of T5 (ndim 6), T6 (7) or T7 (7) at points x
+extern "C" void orc_halo_integrand(const orc_tables* t, const orc_cov_params* p, int term, const double* th,
+                                   double lMax, const double* x, long n, double* out) {
+  ensure_halo(t);
+  HaloCtx c{t, p, {th[0], th[1], th[2], th[3], th[4], th[5]}, lMax};
+  if (term == 5) integrand_T5_v(6, (size_t)n, x, &c, 1, out);
+  else if (term == 6) integrand_T6_v(7, (size_t)n, x, &c, 1, out);
+  else integrand_T7_v(7, (size_t)n, x, &c, 1, out);
+}
+
+// T5 (:1199-1231, infinite survey), T6 (:1233-1276, square or rectangle: the
+// 1-D T2 part-1 integral of (theta1, theta2) times a 7-D integral), T7
+// (:1278-1313, infinite). relTol <= 0 selects the reference's tolerance (1e-2,
+// 1e-1, 1e-1); maxEval 0 = unbounded, as the reference passes.
+extern "C" double orc_T_halo(const orc_tables* t, const orc_cov_params* p, int term, const double* th, double relTol,
+                             long maxEval, double* err_out, long* neval) {
+  ensure_halo(t);
+  double tmin123 = std::min({th[0], th[1], th[2]}), tmin456 = std::min({th[3], th[4], th[5]});
+  double lMax = 10. / (term == 7 ? std::min(tmin123, tmin456) : std::max(tmin123, tmin456));
+  HaloCtx c{t, p, {th[0], th[1], th[2], th[3], th[4], th[5]}, lMax};
+  const double mmin = pow(10, LOGMMIN), mmax = pow(10, LOGMMAX);
+  const double ll = log(HALO_LMIN), lh = log(lMax);
+  double res = 0, err = 0;
+  if (term == 5) {
+    double xmin[6] = {ll, ll, ll, 0, 0, mmin}, xmax[6] = {lh, lh, lh, 2 * PI, 2 * PI, mmax};
+    orc_hcubature_v(1, integrand_T5_v, &c, 6, xmin, xmax, (size_t)maxEval, 0, relTol > 0 ? relTol : 1e-2,
+                    ORC_ERROR_L1, &res, &err);
+    const double s = 1 / p->area / pow(2 * PI, 5);
+    res *= s, err *= s;
+  } else if (term == 6) {
+    double xmin[7] = {ll, ll, ll, 0, 0, 0, mmin}, xmax[7] = {lh, lh, lh, 2 * PI, 2 * PI, 2 * PI, mmax};
+    orc_hcubature_v(1, integrand_T6_v, &c, 7, xmin, xmax, (size_t)maxEval, 0, relTol > 0 ? relTol : 1e-1,
+                    ORC_ERROR_L1, &res, &err);
+    const long nev7 = orc_last_neval();
+    // integral over ell_1: integrand_T2_part1 over [lMin, lMax] (:1247-1255)
+    T2Ctx a{t, p, th[0], th[1], 1};
+    orc_cov_params q = *p;
+    q.lMin = 0;  // the device cut (dev_lMin) stays at the driver's 0
+    a.p = &q;
+    double vmin1[1] = {HALO_LMIN}, vmax1[1] = {lMax}, rA, eA;
+    orc_hcubature_v(1, integrand_T2_v, &a, 1, vmin1, vmax1, 0, 0, 1e-4, ORC_ERROR_L1, &rA, &eA);
+    rA /= 2 * PI;
+    const double s = rA / pow(2 * PI, 6);
+    res *= s, err *= fabs(s);
+    if (neval) *neval = nev7;
+    if (err_out) *err_out = err;
+    return res;
+  } else {
+    double xmin[7] = {ll, ll, ll, ll, 0, 0, mmin}, xmax[7] = {lh, lh, lh, lh, 2 * PI, 2 * PI, mmax};
+    orc_hcubature_v(1, integrand_T7_v, &c, 7, xmin, xmax, (size_t)maxEval, 0, relTol > 0 ? relTol : 1e-1,
+                    ORC_ERROR_L1, &res, &err);
+    const double s = 1 / p->area / pow(2 * PI, 6);
+    res *= s, err *= s;
+  }
+  if (neval) *neval = orc_last_neval();
+  if (err_out) *err_out = err;
+  return res;
+}
+
+// T5_total (:685-845), T6_total (:847-1024), T7_total (:1026-1044) as sums
+// of (multiplicity, argument pattern) over (a0, a1, a2, b0, b1, b2).
+// T5_total tests a0 == a1 twice (:703-705), so with a0 == a1 the first
+// triplet is taken as (a0, a0, a0) whatever a2 is; the reference's outputs
+// are defined by that.
+extern "C" int orc_halo_total_terms(int term, const double* A, const double* B, int* mult, int* idx) {
+  struct P {
+    int m, i[6];
+  };
+  std::vector<P> v;
+  auto set = [&](std::initializer_list<P> l) {
+    v.clear();
+    for (const P& e : l) v.push_back(e);
+  };
+  const double a0 = A[0], a1 = A[1], a2 = A[2], b0 = B[0], b1 = B[1], b2 = B[2];
+  if (term == 7) {
+    set({{1, {0, 1, 2, 3, 4, 5}}});
+  } else if (term == 5) {
+    if (a0 == a1) {
+      if (b0 == b1 && b0 == b2) set({{9, {0, 0, 0, 3, 3, 3}}});
+      else if (b0 == b1) set({{6, {0, 0, 0, 3, 3, 5}}, {3, {0, 0, 0, 5, 3, 3}}});
+      else if (b1 == b2) set({{3, {0, 0, 0, 3, 4, 4}}, {6, {0, 0, 0, 4, 3, 4}}});
+      else set({{3, {0, 0, 0, 3, 4, 5}}, {3, {0, 0, 0, 4, 3, 5}}, {3, {0, 0, 0, 5, 3, 4}}});
+    } else if (b0 == b1 && b0 == b2) {
+      set({{3, {0, 1, 2, 3, 3, 3}}, {3, {1, 0, 2, 3, 3, 3}}, {3, {2, 0, 1, 3, 3, 3}}});
+    } else if (b0 == b1) {
+      set({{2, {0, 1, 2, 3, 3, 5}}, {1, {0, 1, 2, 5, 3, 3}}, {2, {1, 0, 2, 3, 4, 5}},
+           {1, {1, 0, 2, 5, 3, 3}}, {2, {2, 0, 1, 3, 3, 5}}, {1, {2, 0, 1, 5, 3, 3}}});
+    } else if (b1 == b2) {
+      set({{1, {0, 1, 2, 3, 4, 4}}, {2, {0, 1, 2, 4, 3, 4}}, {1, {1, 0, 2, 3, 4, 4}},
+           {2, {1, 0, 2, 4, 3, 4}}, {1, {2, 0, 1, 3, 4, 4}}, {2, {2, 0, 1, 4, 3, 4}}});
+    } else {
+      for (auto f : {std::array<int, 3>{0, 1, 2}, {1, 0, 2}, {2, 0, 1}})
+        for (auto s : {std::array<int, 3>{3, 4, 5}, {4, 3, 5}, {5, 3, 4}}) v.push_back({1, {f[0], f[1], f[2], s[0], s[1], s[2]}});
+    }
+  } else if (term == 6) {
+    if (a0 == a1 && a0 == a2) {
+      if (b0 == b1 && b0 == b2) set({{3, {0, 0, 0, 3, 3, 3}}, {3, {3, 3, 0, 0, 0, 3}}});
+      else if (b0 == b1) set({{3, {0, 0, 0, 3, 3, 5}}, {1, {3, 3, 0, 0, 0, 5}}, {2, {3, 5, 0, 0, 0, 3}}});
+      else if (b1 == b2) set({{3, {0, 0, 0, 3, 4, 4}}, {2, {3, 4, 0, 0, 0, 4}}, {1, {4, 4, 0, 0, 0, 3}}});
+      else set({{3, {0, 0, 0, 3, 4, 5}}, {1, {3, 4, 0, 0, 0, 5}}, {1, {3, 5, 0, 0, 0, 4}}, {1, {4, 5, 0, 0, 0, 3}}});
+    } else if (a0 == a1) {
+      if (b0 == b1 && b0 == b2) set({{1, {0, 0, 2, 3, 3, 3}}, {2, {0, 2, 0, 3, 3, 3}}, {3, {3, 3, 0, 0, 2, 3}}});
+      else if (b0 == b1)
+        set({{1, {0, 0, 2, 3, 3, 5}}, {2, {0, 2, 0, 3, 3, 5}}, {1, {3, 3, 0, 0, 2, 5}}, {2, {3, 5, 0, 0, 2, 3}}});
+      else if (b1 == b2)
+        set({{1, {0, 0, 2, 3, 4, 4}}, {2, {0, 2, 0, 3, 4, 4}}, {2, {3, 4, 0, 0, 2, 4}}, {1, {4, 4, 0, 0, 2, 3}}});
+      else
+        set({{1, {0, 0, 2, 3, 4, 5}}, {2, {0, 2, 0, 3, 4, 5}}, {1, {3, 4, 0, 0, 2, 5}},
+             {1, {3, 5, 0, 0, 2, 4}}, {1, {4, 5, 0, 0, 2, 3}}});
+    } else if (b0 == b1 && b0 == b2) {
+      set({{1, {0, 1, 2, 3, 3, 3}}, {1, {0, 2, 1, 3, 3, 3}}, {1, {1, 2, 0, 3, 3, 3}}, {3, {3, 3, 0, 1, 2, 3}}});
+    } else if (b0 == b1) {
+      set({{1, {0, 1, 2, 3, 3, 5}}, {1, {0, 2, 1, 3, 3, 5}}, {1, {1, 2, 0, 3, 3, 5}},
+           {1, {3, 3, 0, 1, 2, 5}}, {2, {3, 5, 0, 1, 2, 3}}});
+    } else if (b1 == b2) {
+      set({{1, {0, 1, 2, 3, 4, 4}}, {1, {0, 2, 1, 3, 4, 4}}, {1, {1, 2, 0, 3, 4, 4}},
+           {2, {3, 4, 0, 1, 2, 4}}, {1, {4, 4, 0, 1, 2, 3}}});
+    } else {
+      set({{1, {0, 1, 2, 3, 4, 5}}, {1, {0, 2, 1, 3, 4, 5}}, {1, {1, 2, 0, 3, 4, 5}},
+           {1, {3, 4, 0, 1, 2, 5}}, {1, {3, 5, 0, 1, 2, 4}}, {1, {4, 5, 0, 1, 2, 3}}});
+    }
+  } else {
+    return -1;
+  }
+  for (size_t k = 0; k < v.size(); ++k) {
+    mult[k] = v[k].m;
+    for (int j = 0; j < 6; ++j) idx[6 * k + j] = v[k].i[j];
+  }
+  return (int)v.size();
+}
+
+// T5/T6/T7 totals with each distinct argument set integrated once
+extern "C" double orc_T_halo_total(const orc_tables* t, const orc_cov_params* p, int term, const double* A,
+                                   const double* B, double relTol, long maxEval) {
+  if (term == 6 && p->type == 2) return 0;  // T6_total, :849-850
+  int mult[16], idx[96];
+  int n = orc_halo_total_terms(term, A, B, mult, idx);
+  const double src[6] = {A[0], A[1], A[2], B[0], B[1], B[2]};
+  double r = 0;
+  for (int k = 0; k < n; ++k) {
+    double th[6];
+    for (int j = 0; j < 6; ++j) th[j] = src[idx[6 * k + j]];
+    r += mult[k] * orc_T_halo(t, p, term, th, relTol, maxEval, nullptr, nullptr);
   }
   return r;
 }

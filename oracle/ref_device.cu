@@ -3,10 +3,10 @@
 // refdev REF=<reference cuda_version directory>` into oracle/_ref/ as a
 // device-only cubin, never shipped, never linked into the product).
 //
-// It compiles the reference's cuda_version/bispectrum.cu and gamma.cu as they
-// are (the GSL host routines of gamma.cu are declared by oracle/gsl_stub and
-// never called) and adds two kernels that call the reference's __device__
-// functions at caller-given points:
+// It compiles the reference's cuda_version/bispectrum.cu, gamma.cu and
+// halomodel.cu as they are (the GSL host routines of gamma.cu are declared by
+// oracle/gsl_stub and never called) and adds kernels that call the
+// reference's __device__ functions at caller-given points:
 //   ref_node_eval    bispec(ell/f_K(z), z, idx, didx) (bispectrum.cu:221-291) and
 //                    integrand_bkappa(z, ell) (:311-333), idx/didx/f_K formed as
 //                    integrand_bkappa forms them (:320-324)
@@ -14,6 +14,9 @@
 //                    full_integrand_gamma0/1 (gamma.cu:419-482) at (z, phi, psi),
 //                    reduced in the pairwise order of compute_integrand_gamma0/1's
 //                    shared-memory reduction (:267-363)
+//   ref_halo_los     the one-halo line-of-sight tri- and pentaspectrum
+//                    (halomodel.cu:430-510) with the mass tables the
+//                    reference's host code built
 // The host uploads the constants that copyConstants / set_cosmology /
 // compute_weights_bessel would upload (bispectrum.cu:90-219, gamma.cu:13-56),
 // from tables the reference's own host code built (oracle/ref_harness.cu).
@@ -23,6 +26,22 @@
 // (bispectrum.cu:356-359, 389-392, 421-424), and z = z_max reads index 256.
 #include "bispectrum.cu"
 #include "gamma.cu"
+#include "halomodel.cu"
+
+// halomodel.cu's device code reads this survey-variance table, which
+// apertureStatisticsCovariance.cu defines; that file is not compiled here.
+__constant__ double dev_sigma2_from_windowfunction_array[n_redshift_bins];
+
+// trispectrum_limber_integrated(0, z_max, m, l1..l4) and
+// pentaspectrum_limber_integrated(0, z_max, m, l1..l6) (halomodel.cu:430-510)
+// at rows pts[n][7] = (m, l1, ..., l6)
+extern "C" __global__ void ref_halo_los(const double* pts, int n, double* tri, double* penta) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double* p = pts + 7 * i;
+  tri[i] = trispectrum_limber_integrated(0, dev_z_max, p[0], p[1], p[2], p[3], p[4]);
+  penta[i] = pentaspectrum_limber_integrated(0, dev_z_max, p[0], p[1], p[2], p[3], p[4], p[5], p[6]);
+}
 
 extern "C" __global__ void ref_node_eval(const double* ell, const double* z, int n_tri, int n_z, double* bis,
                                          double* integ) {

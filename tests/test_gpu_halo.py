@@ -1,0 +1,156 @@
+"""The halo-model covariance terms T5, T6, T7 on the GPU against the oracle
+(and, where the fixture exists, against the reference's own device code)."""
+import os
+
+import numpy as np
+import pytest
+
+import oracle as O
+from conftest import COSMO1
+
+pytestmark = pytest.mark.gpu
+ARC = O.ARCMIN
+DEG = 0.017453
+SIG, NGAL = 0.3, 10 / ARC ** 2
+TMAX, AREA = 10 * DEG, 100 * DEG * DEG
+TH6 = [8 * ARC, 8 * ARC, 16 * ARC, 8 * ARC, 16 * ARC, 16 * ARC]
+FIXTURE = os.path.join(os.path.dirname(__file__), "golden", "reference_halo.npz")
+# loose tolerances at which the oracle finishes in seconds (the reference's
+# own 1e-2 / 1e-1 / 1e-1 take 1.6e6, >6e6 and 5.5e5 integrand points)
+LOOSE = {5: 0.2, 6: 0.5, 7: 0.3}
+
+
+@pytest.fixture(scope="module")
+def halo_ctx(nz256):
+    import threepoint_gb300 as tp
+
+    ctx = tp.Context(0)
+    ctx.set_shape_noise(SIG, NGAL, False)
+    ctx.set_cosmology(tp.cosmology(**COSMO1), nz256)
+    yield ctx
+    ctx.close()
+
+
+@pytest.fixture(scope="module")
+def halo_oracle(nz256):
+    T = O.Tables(COSMO1, nz256)
+    T.set_noise(SIG, NGAL, False)
+    O.set_threads(0)
+    return T
+
+
+def params(geom):
+    return O.CovParams(geom, TMAX, AREA, 0.0)
+
+
+def test_mass_tables_match_oracle(halo_ctx, halo_oracle):
+    s2, ds2 = halo_ctx.halo_tables()
+    r2, rd2 = halo_oracle.halo_tables()
+    assert np.max(np.abs(s2 / r2 - 1)) < 1e-10
+    assert np.max(np.abs(ds2 / rd2 - 1)) < 1e-10
+
+
+def _points(n=48, seed=3):
+    rng = np.random.default_rng(seed)
+    return np.column_stack([10 ** rng.uniform(9, 17, n), 10 ** rng.uniform(-3, 4, (n, 6))])
+
+
+def test_los_spectra_match_oracle(halo_ctx, halo_oracle):
+    pts = _points()
+    tri, pen = halo_ctx.halo_los(pts)
+    rt, rp = halo_oracle.halo_los(pts)
+    assert np.all(np.isfinite(tri)) and np.all(np.isfinite(pen))
+    np.testing.assert_allclose(tri, rt, rtol=1e-10, atol=0)
+    np.testing.assert_allclose(pen, rp, rtol=1e-10, atol=0)
+
+
+@pytest.mark.skipif(not os.path.exists(FIXTURE), reason="reference halo fixture not generated")
+def test_los_spectra_match_reference_device_code(nz256):
+    """trispectrum_limber_integrated / pentaspectrum_limber_integrated of the
+    reference, compiled from its sources and run on a GB300 (fixture), against
+    the GPU path on the same cosmologies."""
+    import threepoint_gb300 as tp
+
+    f = np.load(FIXTURE)
+    keys = ("h", "sigma8", "omb", "omc", "ns", "w", "om", "ow", "zmax")
+    cos = [dict(zip(keys, c)) for c in f["cosmo"]]
+    with tp.Context(0) as ctx:
+        ctx.set_cosmologies([tp.cosmology(**c) for c in cos], nz256)
+        for ci in range(len(cos)):
+            s2, ds2 = ctx.halo_tables(ci)
+            np.testing.assert_allclose(s2, f["halo"][ci][:128], rtol=1e-10)
+            np.testing.assert_allclose(ds2, f["halo"][ci][128:], rtol=1e-10)
+            tri, pen = ctx.halo_los(f["pts"], cosmo_index=ci)
+            np.testing.assert_allclose(tri, f["tri"][ci], rtol=1e-9, atol=0)
+            np.testing.assert_allclose(pen, f["penta"][ci], rtol=1e-9, atol=0)
+
+
+@pytest.mark.parametrize("term,geom", [(5, 2), (6, 1), (7, 2)])
+def test_integrand_points_match_oracle(halo_ctx, halo_oracle, term, geom):
+    rng = np.random.default_rng(term)
+    n = 64
+    nd = 6 if term == 5 else 7
+    nlog = 4 if term == 7 else 3
+    lmax = 10 / (min(min(TH6[:3]), min(TH6[3:])) if term == 7 else max(min(TH6[:3]), min(TH6[3:])))
+    x = np.column_stack([rng.uniform(np.log(1e-4), np.log(lmax), (n, nlog)),
+                         rng.uniform(0, 2 * np.pi, (n, nd - 1 - nlog)), rng.uniform(1e9, 1e17, n)])
+    got = halo_ctx.halo_integrand(term, TH6, x, geometry=geom, thetaMax=TMAX)
+    ref = halo_oracle.halo_integrand(term, params(geom), TH6, lmax, x)
+    assert np.count_nonzero(ref) > n // 4
+    np.testing.assert_allclose(got, ref, rtol=1e-10, atol=1e-10 * np.max(np.abs(ref)))
+
+
+@pytest.mark.parametrize("term,geom", [(5, 2), (6, 1), (6, 3), (7, 2)])
+def test_terms_match_oracle_loose_tolerance(halo_ctx, halo_oracle, term, geom):
+    """The same adaptive algorithm on the same integrand: the GPU and the oracle
+    refine the same regions, so the values agree far inside the tolerance."""
+    small = 5 * DEG
+    if geom == 3:
+        halo_ctx.set_rectangle_side(small)
+    p = O.CovParams(geom, TMAX, AREA, 0.0, small)
+    halo_ctx.set_cov_tolerance(term, LOOSE[term])
+    try:
+        got = halo_ctx.cov_term(term, TH6, geometry=geom, thetaMax=TMAX, area=AREA)[0]
+    finally:
+        halo_ctx.set_cov_tolerance(term, 0.0)
+    ref, err, nev = halo_oracle.cov_T_halo(term, p, TH6, LOOSE[term])
+    assert ref != 0 and abs(err / ref) <= LOOSE[term]
+    assert got == pytest.approx(ref, rel=1e-8)
+
+
+def test_t5_reference_tolerance_matches_oracle(halo_ctx, halo_oracle):
+    """T5 at the reference's 1e-2 (about 1.6e6 integrand points)."""
+    got = halo_ctx.cov_term(5, TH6, geometry=2, thetaMax=TMAX, area=AREA)[0]
+    ref, err, nev = halo_oracle.cov_T_halo(5, params(2), TH6)
+    assert nev > 100000 and abs(err / ref) <= 1e-2
+    assert got == pytest.approx(ref, rel=1e-6)
+
+
+@pytest.mark.parametrize("term,geom", [(5, 2), (6, 1), (7, 2)])
+def test_totals_match_oracle(halo_ctx, halo_oracle, term, geom):
+    """Totals over the reference's argument patterns, including T5_total's
+    repeated th0 == th1 test, at loose tolerances."""
+    a = [8 * ARC, 8 * ARC, 16 * ARC]
+    b = [8 * ARC, 16 * ARC, 16 * ARC]
+    halo_ctx.set_cov_tolerance(term, LOOSE[term])
+    try:
+        got = halo_ctx.cov_total(term, [a], [b], geometry=geom, thetaMax=TMAX, area=AREA)[0]
+    finally:
+        halo_ctx.set_cov_tolerance(term, 0.0)
+    ref = halo_oracle.cov_total_halo(term, params(geom), a, b, LOOSE[term])
+    assert got == pytest.approx(ref, rel=1e-8)
+
+
+def test_geometry_rules(halo_ctx):
+    import threepoint_gb300 as tp
+
+    with pytest.raises(tp.ThreepointError):
+        halo_ctx.cov_term(5, TH6, geometry=1, thetaMax=TMAX, area=AREA)
+    with pytest.raises(tp.ThreepointError):
+        halo_ctx.cov_term(7, TH6, geometry=3, thetaMax=TMAX, area=AREA)
+    with pytest.raises(tp.ThreepointError):
+        halo_ctx.cov_term(6, TH6, geometry=2, thetaMax=TMAX, area=AREA)
+    with pytest.raises(tp.ThreepointError):
+        halo_ctx.cov_total(6, [TH6[:3]], [TH6[3:]], geometry=0, thetaMax=TMAX, area=AREA)
+    # T6_total is 0 for the infinite survey
+    assert halo_ctx.cov_total(6, [TH6[:3]], [TH6[3:]], geometry=2, thetaMax=TMAX, area=AREA)[0] == 0.0

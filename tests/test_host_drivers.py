@@ -179,14 +179,26 @@ def test_driver_usage_on_wrong_argc(tp, name, nargs):
     assert "Wrong number of command line parameters" in r.stderr
 
 
-def test_cov_driver_rejects_halo_model_terms(tp, tmp_path):
+@pytest.mark.parametrize("flags,geometry,message", [
+    ((0, 0, 1, 0, 0, 0, 0), "square", "T4: Wrong survey geometry"),
+    ((0, 0, 0, 1, 0, 0, 0), "square", "T5: Wrong survey geometry"),
+    ((0, 0, 0, 0, 1, 0, 0), "circle", "T6: Wrong survey geometry"),
+    ((1, 0, 0, 0, 0, 1, 0), "rectangular", "T7: Wrong survey geometry"),
+    ((0, 0, 0, 0, 0, 0, 1), "circle", "T7_SSC: Wrong survey geometry"),
+])
+def test_cov_driver_checks_term_geometries(tp, tmp_path, flags, geometry, message):
+    """Terms coded for some survey geometries only fail before any output, as
+    the reference's driver does when the term throws at the first pair."""
     from threepoint_gb300 import build as B
 
-    r = _run(B.driver("calculateApertureStatisticsCovariance"), "c", "t", "nz", str(tmp_path) + "/", "p",
-             1, 0, 0, 1, 0, 0, 0, "square")
+    p = tmp_path / "cov.param"
+    p.write_text("thetaMax 10\nshapenoise_sigma 0.3\ngalaxy_density 10\nunit arcmin\nshapenoiseOnly 1\narea 100\n")
+    out = tmp_path / "out"
+    out.mkdir()
+    r = _run(B.driver("calculateApertureStatisticsCovariance"), "c", "t", "nz", str(out) + "/", p, *flags, geometry)
     assert r.returncode != 0
-    assert "halo model" in r.stderr
-    assert not os.listdir(tmp_path)
+    assert message in r.stderr
+    assert not os.listdir(out)
 
 
 def test_cov_driver_rejects_unknown_geometry(tp, tmp_path):

@@ -187,3 +187,63 @@ def test_white_noise_covariance_brute_force(nz256, a, b):
     p = O.CovParams(1, side, side * side, 0.0)
     assert T.cov_total(1, p, th123, th456) == pytest.approx(t1, rel=1e-2)
     assert T.cov_total(2, p, th123, th456) == pytest.approx(t2, rel=2e-3)
+
+
+# ---- halo model (cuda_version/halomodel.cu), T5 / T6 / T7 ------------------
+def test_halo_tables_match_reference(oracle_tables):
+    """sigma^2(m) and dsigma^2/dm tables of setSigma2 / setdSigma2dm: the
+    oracle's restatement on its own cubature equals the reference's host code."""
+    s2, ds2 = oracle_tables.halo_tables()
+    assert np.array_equal(s2, np.array(GOLD["halo_tables"]["sig2"]))
+    assert np.array_equal(ds2, np.array(GOLD["halo_tables"]["dsig2"]))
+
+
+def test_halo_functions_match_reference(oracle_tables):
+    T = oracle_tables
+    for m, z, v in GOLD["hmf"]:
+        assert T.hmf(m, z) == pytest.approx(v, rel=1e-13)
+    for m, z, s2, ds2 in GOLD["get_sigma2"]:
+        assert T.get_sigma2(m, z) == pytest.approx(s2, rel=1e-14)
+        assert T.get_dsigma2(m, z) == pytest.approx(ds2, rel=1e-14)
+    for k, m, z, v in GOLD["u_NFW"]:
+        assert T.u_nfw(k, m, z) == pytest.approx(v, rel=1e-14, abs=1e-300)
+    for m, z, c, r in GOLD["concentration"]:
+        assert O.lib().orc_concentration(m, z) == c
+        assert T.r_200(m) == r
+    for x, si, ci in GOLD["SiCi"]:
+        assert O.sici(x) == (si, ci)
+
+
+def test_halo_cubature_bit_identical_to_reference(oracle_tables):
+    """The reference's own hcubature_v on the oracle's T5 / T6 / T7 integrands
+    (6-D and 7-D, loose tolerances) gives the oracle's value bit for bit."""
+    T = oracle_tables
+    deg = 0.017453
+    for g in GOLD["halo_ref_cubature"]:
+        T.set_noise(g["sigma"], g["n_arcmin2"] / O.ARCMIN ** 2, False)
+        par = O.CovParams(g["geometry"], g["thetaMax_deg"] * deg, g["area_deg2"] * deg * deg, 0.0)
+        th6 = [x * O.ARCMIN for x in g["theta_arcmin"]]
+        h = O.lib().orc_halo_ctx_create(T._h, C.byref(par), g["term"], O._dp(np.array(th6)))
+        lmax = O.lib().orc_halo_ctx_lmax(h)
+        nlog = 4 if g["term"] == 7 else 3
+        ndim = 6 if g["term"] == 5 else 7
+        xmin = np.array([math.log(1e-4)] * nlog + [0.0] * (ndim - 1 - nlog) + [1e9])
+        xmax = np.array([math.log(lmax)] * nlog + [2 * math.pi] * (ndim - 1 - nlog) + [1e17])
+        v, e = np.zeros(1), np.zeros(1)
+        fp = C.cast(O.lib().orc_integrand_halo_v, C.c_void_p).value
+        O.lib().orc_hcubature_v(1, C.c_void_p(fp), h, ndim, O._dp(xmin), O._dp(xmax), 0, 0, g["rel"], 3, O._dp(v),
+                                O._dp(e))
+        O.lib().orc_halo_ctx_destroy(h)
+        assert v[0] == g["raw_value"] and e[0] == g["raw_err"], g["term"]
+    T.set_noise(0.0, 1.0, False)  # the fixture's default
+
+
+def test_halo_total_terms_follow_reference_branches():
+    """T5_total tests th0 == th1 twice, so (a, a, b) is integrated as (a, a, a);
+    T6_total's case E and T7_total's single ordering."""
+    a, b, c = 1.0, 2.0, 3.0
+    assert O.halo_total_terms(5, [a, a, b], [c, c, c]) == [(9, (0, 0, 0, 3, 3, 3))]
+    assert sum(m for m, _ in O.halo_total_terms(5, [a, b, c], [a, b, c])) == 9
+    assert O.halo_total_terms(6, [a, a, b], [c, c, c]) == [(1, (0, 0, 2, 3, 3, 3)), (2, (0, 2, 0, 3, 3, 3)),
+                                                          (3, (3, 3, 0, 0, 2, 3))]
+    assert O.halo_total_terms(7, [a, b, c], [c, b, a]) == [(1, (0, 1, 2, 3, 4, 5))]

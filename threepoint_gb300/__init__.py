@@ -182,6 +182,10 @@ def lib():
         L.tp_cov_total_batch.argtypes = [p, i, i, i, d, d, dp, dp, i, i, dp, ip]
         L.tp_cov_term_batch.argtypes = [p, i, i, i, d, d, dp, i, i, dp, ip]
         L.tp_set_rectangle_side.argtypes = [p, d]
+        L.tp_halo_tables.argtypes = [p, i, dp]
+        L.tp_halo_los.argtypes = [p, i, dp, l, dp, dp]
+        L.tp_halo_integrand_points.argtypes = [p, i, i, i, d, dp, dp, l, dp]
+        L.tp_ctx_set_cov_tolerance.argtypes = [p, i, d]
         L.tp_cov_params_from_file.argtypes = [C.c_char_p, C.POINTER(_CovParams)]
         L.tp_gamma_config_from_file.argtypes = [C.c_char_p, C.POINTER(_GammaConfig)]
         L.tp_gamma_triangles.argtypes = [C.POINTER(_GammaConfig), dp, dp]
@@ -469,10 +473,11 @@ class Context:
     # -- covariance (cuda_version/apertureStatisticsCovariance.cu:272-683) --
     def cov_total(self, term, th123, th456, geometry=GEOM_SQUARE, thetaMax=0.0, area=0.0, precision=FP64,
                   cosmo_index=0, check=True):
-        """T1_total / T2_total / T4_total for pairs of triplets
-        (apertureStatisticsCovariance.cu:272-683). With check=False an
-        integral that hit its region or sweep cap does not raise; the number of
-        such integrals is left in self.last_capped."""
+        """T1_total / T2_total / T4_total / T5_total / T6_total / T7_total for
+        pairs of triplets (apertureStatisticsCovariance.cu:272-1044). With
+        check=False an integral that hit its region or sweep cap does not
+        raise; the number of such integrals is left in self.last_capped. The
+        halo-model terms 5-7 are evaluated in FP64 for either precision."""
         a = _arr(th123).reshape(-1, 3)
         b = _arr(th456).reshape(-1, 3)
         out = np.zeros(len(a))
@@ -485,7 +490,8 @@ class Context:
         return out
 
     def cov_term(self, term, th6, geometry=GEOM_SQUARE, thetaMax=0.0, area=0.0, precision=FP64, cosmo_index=0):
-        """Single terms T1/T2/T4(theta1..theta6) (apertureStatisticsCovariance.cu:1065-1197)."""
+        """Single terms T1/T2/T4/T5/T6/T7(theta1..theta6)
+        (apertureStatisticsCovariance.cu:1065-1313)."""
         t = _arr(th6).reshape(-1, 6)
         out = np.zeros(len(t))
         nb = C.c_int(0)
@@ -501,6 +507,46 @@ class Context:
 
     def T4_total(self, th123, th456, **kw):
         return float(self.cov_total(4, [th123], [th456], **kw)[0])
+
+    def T5_total(self, th123, th456, **kw):
+        return float(self.cov_total(5, [th123], [th456], **kw)[0])
+
+    def T6_total(self, th123, th456, **kw):
+        return float(self.cov_total(6, [th123], [th456], **kw)[0])
+
+    def T7_total(self, th123, th456, **kw):
+        return float(self.cov_total(7, [th123], [th456], **kw)[0])
+
+    # -- halo model (cuda_version/halomodel.cu) --
+    def set_cov_tolerance(self, term, rel_tol):
+        """Relative tolerance of the T5/T6/T7 integrals (0 = the reference's
+        1e-2 / 1e-1 / 1e-1)."""
+        _check(self._h, lib().tp_ctx_set_cov_tolerance(self._h, term, rel_tol))
+
+    def halo_tables(self, cosmo_index=0):
+        """(sigma^2(m_i), dsigma^2/dm(m_i)) at z = 0, 128 masses each."""
+        out = np.zeros(256)
+        _check(self._h, lib().tp_halo_tables(self._h, cosmo_index, _dp(out)))
+        return out[:128].copy(), out[128:].copy()
+
+    def halo_los(self, pts, cosmo_index=0):
+        """One-halo line-of-sight trispectrum (l1..l4) and pentaspectrum
+        (l1..l6) at rows (m, l1, ..., l6)."""
+        pts = _arr(pts).reshape(-1, 7)
+        tri, pen = np.zeros(len(pts)), np.zeros(len(pts))
+        _check(self._h, lib().tp_halo_los(self._h, cosmo_index, _dp(pts), len(pts), _dp(tri), _dp(pen)))
+        return tri, pen
+
+    def halo_integrand(self, term, th6, x, geometry=GEOM_INFINITE, thetaMax=0.0, cosmo_index=0):
+        """Integrand of T5 (rows of 6) / T6, T7 (rows of 7) at points x, before
+        the 1/area/(2 pi)^n normalisation."""
+        nd = 6 if term == 5 else 7
+        x = _arr(x).reshape(-1, nd)
+        th = _arr(th6)
+        out = np.zeros(len(x))
+        _check(self._h, lib().tp_halo_integrand_points(self._h, cosmo_index, term, geometry, thetaMax, _dp(th),
+                                                        _dp(x), len(x), _dp(out)))
+        return out
 
 
 class Likelihood:

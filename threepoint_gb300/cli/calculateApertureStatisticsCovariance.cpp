@@ -6,10 +6,18 @@
 //   calculateApertureStatisticsCovariance.x cosmo.dat thetas.dat nz.dat outfolder/ cov_param.dat
 //       T1 T2 T4 T5 T6 T7 T7_2h circle|square|infinite|rectangular [fp32]
 //
-// T5, T6, T7 and T7_2h are the reference's halo-model terms, which this
-// library does not provide: requesting one is an error. Output per term:
-// outfolder + cov_<geometry>_term<k>Numerical_sigma_<s>_n_<n>_thetaMax_<t>_gpu.dat,
-// an N x N symmetric matrix, one row per line, each value followed by a space.
+// T5, T6 and T7 are the halo-model terms (FP64 whatever the precision
+// argument). T7_2h is identically zero in the reference: its integrand
+// (pentaspectrum_integrand_ssc, halomodel.cu:469-496) multiplies by the survey
+// variance table dev_sigma2_from_windowfunction_array, which nothing in the
+// reference fills (zero-initialised constant memory,
+// apertureStatisticsCovariance.cu:28), so its hcubature_v returns 0 after the
+// first region; this driver writes those zeros for the square and infinite
+// geometries and fails for the others, as the reference throws there
+// (:1340-1353). Output per term:
+// outfolder + cov_<geometry>_term<k>Numerical_sigma_<s>_n_<n>_thetaMax_<t>_gpu.dat
+// (T7_2h: ..._term7_2h_Numerical_...), an N x N symmetric matrix, one row per
+// line, each value followed by a space.
 #include <cstring>
 #include <fstream>
 #include <stdexcept>
@@ -61,11 +69,6 @@ int main(int argc, char* argv[]) {
   for (int i = 0; i < 7; ++i) calc[i] = std::stoi(argv[6 + i]) != 0;
   const char* names[7] = {"term1", "term2", "term4", "term5", "term6", "term7", "term7 (2h)"};
   for (int i = 0; i < 7; ++i) std::cerr << "Calculating " << names[i] << ":" << calc[i] << std::endl;
-  for (int i = 3; i < 7; ++i)
-    if (calc[i])
-      cli::die(std::string("Calculating ") + names[i] +
-                   " needs the halo model (T5, T6, T7, T7_2h), which this library does not provide",
-               -1);
   const int precision = argc == 15 ? TP_FP32 : TP_FP64;
 
   std::cerr << "Using cosmology from " << cosmo_file << std::endl;
@@ -85,6 +88,17 @@ int main(int argc, char* argv[]) {
   else if (type_str == "rectangular") geom = TP_GEOM_RECTANGLE;
   else cli::die("Cov type not correctly specified", -1);
   std::cerr << "Using survey geometry " << type_str << std::endl;
+  // terms coded for some geometries only: the reference throws at the first
+  // pair, before any output is written (apertureStatisticsCovariance.cu:1193,
+  // 1227, 1237, 1314, 1351); T6_total and T7_2h_total return 0 for the
+  // infinite survey before reaching those checks (:849-850, :1048-1049)
+  if (calc[2] && geom != TP_GEOM_INFINITE) cli::die("T4: Wrong survey geometry, only coded for infinite survey", -1);
+  if (calc[3] && geom != TP_GEOM_INFINITE) cli::die("T5: Wrong survey geometry, only coded for infinite survey", -1);
+  if (calc[4] && geom == TP_GEOM_CIRCLE)
+    cli::die("T6: Wrong survey geometry, only coded for square and rectangular survey", -1);
+  if (calc[5] && geom != TP_GEOM_INFINITE) cli::die("T7: Wrong survey geometry, only coded for infinite survey", -1);
+  if (calc[6] && (geom == TP_GEOM_CIRCLE || geom == TP_GEOM_RECTANGLE))
+    cli::die("T7_SSC: Wrong survey geometry, only coded for square survey", -1);
 
   tp_ctx* ctx = cli::make_context(cosmo_file, nz_file, 0, nullptr);
   cli::check(tp_set_shape_noise(ctx, par.shapenoise_sigma, par.galaxy_density, par.shapenoise_only),
@@ -117,20 +131,26 @@ int main(int argc, char* argv[]) {
   char filename[255];
   const double n_deg = par.galaxy_density / cli::rad_to_deg(1) / cli::rad_to_deg(1);
   const double theta_max_deg = cli::rad_to_deg(par.theta_max);
-  const int terms[3] = {1, 2, 4};
-  for (int q = 0; q < 3; ++q) {
+  const int terms[7] = {1, 2, 4, 5, 6, 7, 72};
+  for (int q = 0; q < 7; ++q) {
     if (!calc[q]) continue;
-    std::vector<double> cov(npair);
-    int ncap = 0;
-    int st = tp_cov_total_batch(ctx, 0, terms[q], geom, par.theta_max, par.area, a.data(), b.data(), npair, precision,
-                                cov.data(), &ncap);
-    if (st == TP_ERR_CAPACITY)
-      std::cerr << "warning: " << tp_last_error(ctx) << std::endl;
-    else
-      cli::check(st, std::string("T") + std::to_string(terms[q]), ctx);
-    snprintf(filename, sizeof(filename), "cov_%s_term%dNumerical_sigma_%.2f_n_%.2f_thetaMax_%.2f_gpu.dat",
-             type_str.c_str(), terms[q], par.shapenoise_sigma, n_deg, theta_max_deg);
-    std::cerr << "Writing Term" << terms[q] << " to " << out_folder + filename << std::endl;
+    std::vector<double> cov(npair, 0.0);
+    if (terms[q] == 72) {
+      // T7_2h: zero (see the header comment)
+      snprintf(filename, sizeof(filename), "cov_%s_term7_2h_Numerical_sigma_%.2f_n_%.2f_thetaMax_%.2f_gpu.dat",
+               type_str.c_str(), par.shapenoise_sigma, n_deg, theta_max_deg);
+    } else {
+      int ncap = 0;
+      int st = tp_cov_total_batch(ctx, 0, terms[q], geom, par.theta_max, par.area, a.data(), b.data(), npair,
+                                  precision, cov.data(), &ncap);
+      if (st == TP_ERR_CAPACITY)
+        std::cerr << "warning: " << tp_last_error(ctx) << std::endl;
+      else
+        cli::check(st, std::string("T") + std::to_string(terms[q]), ctx);
+      snprintf(filename, sizeof(filename), "cov_%s_term%dNumerical_sigma_%.2f_n_%.2f_thetaMax_%.2f_gpu.dat",
+               type_str.c_str(), terms[q], par.shapenoise_sigma, n_deg, theta_max_deg);
+    }
+    std::cerr << "Writing " << names[q] << " to " << out_folder + filename << std::endl;
     if (!write_cov(cov, n_ind, out_folder + filename)) {
       std::cerr << "writeCov: Could not open " << out_folder + filename << std::endl;
       std::cerr << "Writing instead to current directory!" << std::endl;

@@ -299,6 +299,9 @@ void tp_ctx::free_cosmo() {
   cudaFree(d_ck32);
   cudaFree(d_plt);
   cudaFree(d_ehg);
+  cudaFree(d_halo);
+  d_halo = nullptr;
+  halo_ready.clear();
   d_cos = nullptr;
   d_eh = nullptr;
   d_tab = nullptr;
@@ -452,6 +455,7 @@ extern "C" int tp_set_cosmologies(tp_ctx* ctx, const tp_cosmology* cosmo, int n,
   }
   ctx->n_cosmo = n;
   ctx->h_cos = hc;
+  ctx->halo_ready.assign(ctx->cosmo_cap, 0);
   cudaStream_t s = ctx->stream;
   e = cudaMemcpyAsync(ctx->d_cos, hc.data(), sizeof(CosmoDev) * n, cudaMemcpyHostToDevice, s);
   if (e == cudaSuccess) e = cudaMemcpyAsync(ctx->d_eh, he.data(), sizeof(EHConst) * n, cudaMemcpyHostToDevice, s);

@@ -50,6 +50,11 @@ struct tp_ctx {
   void* d_ck32 = nullptr;
   float4* d_plt = nullptr;  // [n_cosmo][PLT_N] log2 P_lin cubic segments
   double* d_ehg = nullptr;  // [n_cosmo][EHG_N] 2 ln T(k) of the sigma(R) integrand
+  // halo-model tables (covariance terms T5-T7), built per cosmology on first use
+  tp::HaloTab* d_halo = nullptr;
+  std::vector<char> halo_ready;
+  // relative tolerance of the T5, T6, T7 integrals (index 5..7); 0 = the reference's
+  double cov_rel_tol[8] = {0, 0, 0, 0, 0, 0, 0, 0};
 
   // shape noise of P(ell)
   double sigma_eps = 0.0, ngal = 1.0;

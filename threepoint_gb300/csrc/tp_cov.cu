@@ -28,65 +28,18 @@
 
 #include "tp_bispec.cuh"
 #include "tp_capi_internal.h"
+#include "tp_cov.cuh"
 #include "tp_cubature.cuh"
+#include "tp_halo.h"
 #include "tp_internal.cuh"
 #include "tp_kernels.cuh"
 
 namespace tp {
 
-// P_kappa line-of-sight term of node j at ell (bispectrum.cu:531-600,951-991):
-// W_j * T17(k) * P_nl(k, z_j), k = ell / f_K(z_j).
-template <typename R>
-__device__ __forceinline__ R pell_node(const R* __restrict__ hc, int j, R ell, R l2ell, const CosmoK<R>& K) {
-  typedef Mth<R> M;
-  const R W = hc[HC_W * NNODE + j];
-  if (W == (R)0) return (R)0;
-  const R k = ell * hc[HC_INVFK * NNODE + j];
-  const R l2k = l2ell + hc[HC_L2INVFK * NNODE + j];
-  const R P = plin<R>(K, k * K.h, l2k + K.l2h);
-  const R k3 = k * k * k;
-  const R pl = P * hc[HC_D1SQ * NNODE + j] * k3 * (R)(1.0 / (2 * PI * PI));
-  const R l2y = l2k + hc[HC_L2RS * NNODE + j];
-  const R y = k * hc[HC_RS * NNODE + j];
-  const R ysq = y * y;
-  R ph = hc[HC_A * NNODE + j] * M::ex2((R)3 * hc[HC_F1 * NNODE + j] * l2y) *
-         M::rcp((R)1 + hc[HC_B * NNODE + j] * M::ex2(hc[HC_F2 * NNODE + j] * l2y) +
-                M::ex2(((R)3 - hc[HC_GAM * NNODE + j]) * (hc[HC_L2F3C * NNODE + j] + l2y)));
-  ph = ph * ysq * M::rcp(ysq + hc[HC_XNU * NNODE + j]);
-  const R pq = pl * M::ex2(hc[HC_BETA * NNODE + j] * M::lg2((R)1 + pl)) * M::rcp((R)1 + pl * hc[HC_ALPHA * NNODE + j]) *
-               M::ex2(-(y * (R)0.25 + ysq * (R)0.125) * (R)1.4426950408889634);
-  const R pnl = (R)(2 * PI * PI) * (pq + ph) * M::rcp(k3);
-  // T17 correction (bispectrum.cu:971-979)
-  const R a1 = (R)1.3063, a2 = (R)1.1475, a3 = (R)0.62793, c1 = (R)9.5171e-4, c2 = (R)5.1543e-3;
-  const R corr = M::ex2(a1 * M::lg2((R)1 + c1 * M::ex2(-a1 * l2k)) - a3 * M::lg2((R)1 + c2 * M::ex2(-a2 * l2k)));
-  return W * corr * pnl;
-}
-
-// windows of the survey geometries (apertureStatisticsCovariance.cu:117-153)
-// G_square is the rectangle with two equal sides; G_rectangle (:154-172) has
-// side thetaMax along lx and thetaMax_smaller along ly
-template <typename R>
-__device__ inline R g_square(R thetaMax, R thetaMaxY, R lx, R ly) {
-  R t1 = (R)0.5 * lx * thetaMax, t2 = (R)0.5 * ly * thetaMaxY;
-  R j1 = fabs(t1) <= (R)1e-6 ? (R)1 : sin(t1) / t1;
-  R j2 = fabs(t2) <= (R)1e-6 ? (R)1 : sin(t2) / t2;
-  return j1 * j1 * j2 * j2;
-}
-template <typename R>
-__device__ inline R g_circle(R thetaMax, R ell) {
-  R t = thetaMax * ell;
-  R r = j1(t);
-  return r * r * (R)4 / (t * t);
-}
-
 // ---------------------------------------------------------------------------
 // Integrals whose integrand is a weight times a product of P(ell) values
 enum PellKind { K_T1_SQUARE = 0, K_T1_CIRCLE, K_T1_INF, K_T2_A, K_T2_B_SQUARE, K_T2_B_CIRCLE };
 
-struct CovJob {
-  double th[6];
-  double lmin, lmax;
-};
 
 template <typename R, int DIM, int KIND>
 struct PellProd {
@@ -392,46 +345,6 @@ struct BkProd {
   }
 };
 
-template <int DIM, class P, int NT>
-__global__ void __launch_bounds__(NT) k_cov(P pol_in, int njobs, int* job_counter, EngineCfg cfg, char* scratch,
-                                            size_t slot_bytes) {
-  P pol = pol_in;
-  pol.loaded = 0;
-  adaptive_body<DIM, 1, NT, P>(pol, njobs, job_counter, cfg, scratch, slot_bytes);
-}
-
-template <int DIM, class P>
-static int run_engine(tp_ctx* ctx, const P& pol, int njobs, double rel_tol) {
-  constexpr int NT = 256;
-  if (njobs == 0) return TP_OK;
-  size_t smem = engine_smem_bytes<DIM, 1, P>();
-  cudaError_t e = cudaFuncSetAttribute(k_cov<DIM, P, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (e != cudaSuccess) return tp_cuda(ctx, e, "cov attribute");
-  int sms = 0, per_sm = 0;
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
-  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cov<DIM, P, NT>, NT, smem);
-  if (e != cudaSuccess || per_sm < 1) return tp_cuda(ctx, e ? e : cudaErrorInvalidConfiguration, "cov occupancy");
-  int grid = sms * per_sm;
-  if (ctx->max_ctas > 0 && grid > ctx->max_ctas) grid = ctx->max_ctas;
-  if (grid > njobs) grid = njobs;
-  // covariance integrals (6-D square-window T1, oscillating 2-D T2) refine to
-  // 10^5 regions and more: at least 2^19 regions per integral, with the grid
-  // trimmed so that the region stores stay within 64 GB of HBM
-  const int cap = std::max(ctx->region_cap, 1 << 19);
-  size_t slot = Slot<DIM, 1>::bytes(cap);
-  const size_t budget = size_t(64) << 30;
-  if ((size_t)grid * slot > budget) grid = std::max(1, (int)(budget / slot));
-  int st = ctx->ensure_scratch((size_t)grid * slot);
-  if (st) return st;
-  EngineCfg cfg{0.0, rel_tol, TP_NORM_L1, cap, 4000};
-  e = cudaMemsetAsync(ctx->d_counter, 0, sizeof(int), ctx->stream);
-  if (e == cudaSuccess) {
-    k_cov<DIM, P, NT><<<grid, NT, smem, ctx->stream>>>(pol, njobs, ctx->d_counter, cfg, ctx->d_scratch, slot);
-    e = cudaGetLastError();
-  }
-  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
-  return tp_cuda(ctx, e, "cov launch");
-}
 
 // ---------------------------------------------------------------------------
 // host side: permutation tables of the totals, job assembly
@@ -535,27 +448,64 @@ static std::vector<PermTerm> t4_terms(const double* a, const double* b) {
           {1, {5, 0, 1, 2, 3, 4}}, {1, {5, 0, 2, 1, 3, 4}}, {1, {5, 1, 2, 0, 3, 4}}};
 }
 
-// distinct integrals of one kind
-struct JobSet {
-  std::vector<CovJob> jobs;
-  std::map<std::vector<double>, int> index;
-  int add(const double* th, int nth, double lmin, double lmax) {
-    std::vector<double> key(th, th + nth);
-    key.push_back(lmin);
-    key.push_back(lmax);
-    auto it = index.find(key);
-    if (it != index.end()) return it->second;
-    CovJob j;
-    memset(&j, 0, sizeof(j));
-    for (int i = 0; i < nth; ++i) j.th[i] = th[i];
-    j.lmin = lmin;
-    j.lmax = lmax;
-    int id = (int)jobs.size();
-    jobs.push_back(j);
-    index[key] = id;
-    return id;
+
+// T5_total, apertureStatisticsCovariance.cu:685-845. Its second test repeats
+// th0 == th1 (:703-705), so whenever th0 == th1 the first triplet is taken as
+// (th0, th0, th0); the reference's outputs are defined by that.
+static std::vector<PermTerm> t5_terms(const double* a, const double* b) {
+  const bool b01 = b[0] == b[1], b12 = b[1] == b[2], b02 = b[0] == b[2];
+  if (a[0] == a[1]) {
+    if (b01 && b02) return {{9, {0, 0, 0, 3, 3, 3}}};
+    if (b01) return {{6, {0, 0, 0, 3, 3, 5}}, {3, {0, 0, 0, 5, 3, 3}}};
+    if (b12) return {{3, {0, 0, 0, 3, 4, 4}}, {6, {0, 0, 0, 4, 3, 4}}};
+    return {{3, {0, 0, 0, 3, 4, 5}}, {3, {0, 0, 0, 4, 3, 5}}, {3, {0, 0, 0, 5, 3, 4}}};
   }
-};
+  if (b01 && b02) return {{3, {0, 1, 2, 3, 3, 3}}, {3, {1, 0, 2, 3, 3, 3}}, {3, {2, 0, 1, 3, 3, 3}}};
+  if (b01)
+    return {{2, {0, 1, 2, 3, 3, 5}}, {1, {0, 1, 2, 5, 3, 3}}, {2, {1, 0, 2, 3, 4, 5}},
+            {1, {1, 0, 2, 5, 3, 3}}, {2, {2, 0, 1, 3, 3, 5}}, {1, {2, 0, 1, 5, 3, 3}}};
+  if (b12)
+    return {{1, {0, 1, 2, 3, 4, 4}}, {2, {0, 1, 2, 4, 3, 4}}, {1, {1, 0, 2, 3, 4, 4}},
+            {2, {1, 0, 2, 4, 3, 4}}, {1, {2, 0, 1, 3, 4, 4}}, {2, {2, 0, 1, 4, 3, 4}}};
+  std::vector<PermTerm> out;
+  for (const auto& f : {std::array<int, 3>{0, 1, 2}, {1, 0, 2}, {2, 0, 1}})
+    for (const auto& g : {std::array<int, 3>{3, 4, 5}, {4, 3, 5}, {5, 3, 4}})
+      out.push_back({1, {f[0], f[1], f[2], g[0], g[1], g[2]}});
+  return out;
+}
+
+// T6_total, apertureStatisticsCovariance.cu:847-1024 (cases A-L)
+static std::vector<PermTerm> t6_terms(const double* a, const double* b) {
+  const bool b01 = b[0] == b[1], b12 = b[1] == b[2], b02 = b[0] == b[2];
+  if (a[0] == a[1] && a[0] == a[2]) {
+    if (b01 && b02) return {{3, {0, 0, 0, 3, 3, 3}}, {3, {3, 3, 0, 0, 0, 3}}};
+    if (b01) return {{3, {0, 0, 0, 3, 3, 5}}, {1, {3, 3, 0, 0, 0, 5}}, {2, {3, 5, 0, 0, 0, 3}}};
+    if (b12) return {{3, {0, 0, 0, 3, 4, 4}}, {2, {3, 4, 0, 0, 0, 4}}, {1, {4, 4, 0, 0, 0, 3}}};
+    return {{3, {0, 0, 0, 3, 4, 5}}, {1, {3, 4, 0, 0, 0, 5}}, {1, {3, 5, 0, 0, 0, 4}}, {1, {4, 5, 0, 0, 0, 3}}};
+  }
+  if (a[0] == a[1]) {
+    if (b01 && b02) return {{1, {0, 0, 2, 3, 3, 3}}, {2, {0, 2, 0, 3, 3, 3}}, {3, {3, 3, 0, 0, 2, 3}}};
+    if (b01)
+      return {{1, {0, 0, 2, 3, 3, 5}}, {2, {0, 2, 0, 3, 3, 5}}, {1, {3, 3, 0, 0, 2, 5}}, {2, {3, 5, 0, 0, 2, 3}}};
+    if (b12)
+      return {{1, {0, 0, 2, 3, 4, 4}}, {2, {0, 2, 0, 3, 4, 4}}, {2, {3, 4, 0, 0, 2, 4}}, {1, {4, 4, 0, 0, 2, 3}}};
+    return {{1, {0, 0, 2, 3, 4, 5}}, {2, {0, 2, 0, 3, 4, 5}}, {1, {3, 4, 0, 0, 2, 5}},
+            {1, {3, 5, 0, 0, 2, 4}}, {1, {4, 5, 0, 0, 2, 3}}};
+  }
+  if (b01 && b02)
+    return {{1, {0, 1, 2, 3, 3, 3}}, {1, {0, 2, 1, 3, 3, 3}}, {1, {1, 2, 0, 3, 3, 3}}, {3, {3, 3, 0, 1, 2, 3}}};
+  if (b01)
+    return {{1, {0, 1, 2, 3, 3, 5}}, {1, {0, 2, 1, 3, 3, 5}}, {1, {1, 2, 0, 3, 3, 5}},
+            {1, {3, 3, 0, 1, 2, 5}}, {2, {3, 5, 0, 1, 2, 3}}};
+  if (b12)
+    return {{1, {0, 1, 2, 3, 4, 4}}, {1, {0, 2, 1, 3, 4, 4}}, {1, {1, 2, 0, 3, 4, 4}},
+            {2, {3, 4, 0, 1, 2, 4}}, {1, {4, 4, 0, 1, 2, 3}}};
+  return {{1, {0, 1, 2, 3, 4, 5}}, {1, {0, 2, 1, 3, 4, 5}}, {1, {1, 2, 0, 3, 4, 5}},
+          {1, {3, 4, 0, 1, 2, 5}}, {1, {3, 5, 0, 1, 2, 4}}, {1, {4, 5, 0, 1, 2, 3}}};
+}
+
+// T7_total, apertureStatisticsCovariance.cu:1026-1044: the one ordering
+static std::vector<PermTerm> t7_terms(const double*, const double*) { return {{1, {0, 1, 2, 3, 4, 5}}}; }
 
 template <typename R, int DIM, int KIND>
 static int run_pell_kind(tp_ctx* ctx, int cosmo, const JobSet& js, double theta_max, double theta_max_y,
@@ -699,6 +649,26 @@ static int cov_terms(tp_ctx* ctx, int cosmo, int term, int geom, double theta_ma
     for (size_t i = 0; i < n; ++i) out[i] = ra[i1[i]] * ra[i2[i]] * rb[i3[i]];
     return TP_OK;
   }
+  if (term >= 5) {
+    if (term != 6 && !(area > 0)) return tp_fail(ctx, TP_ERR_ARG, "T5 and T7 need area > 0");
+    int st = halo_terms(ctx, cosmo, term, geom, theta_max, area, th6, out, bad);
+    if (st || term != 6) return st;
+    // T6 = (1-D integral over ell_1 of integrand_T2_part1 with (theta1,
+    // theta2) on [1e-4, lMax], :1247-1255) x its 7-D halo integral; the
+    // integrand's own cut stays at the driver's lMin = 0
+    JobSet ja;
+    std::vector<int> ia(n);
+    for (size_t i = 0; i < n; ++i) {
+      const double* t = th6[i].data();
+      const double a12[2] = {t[0], t[1]};
+      ia[i] = ja.add(a12, 2, HALO_LMIN, halo_lmax(6, t));
+    }
+    std::vector<double> ra;
+    st = run_pell_kind<R, 1, K_T2_A>(ctx, cosmo, ja, theta_max, tmy, 1 / two_pi, 1e-4, ra, bad);
+    if (st) return st;
+    for (size_t i = 0; i < n; ++i) out[i] *= ra[ia[i]];
+    return TP_OK;
+  }
   // term 4: infinite geometry with the survey area
   if (!(area > 0)) return tp_fail(ctx, TP_ERR_ARG, "T4 needs area > 0");
   JobSet js;
@@ -747,11 +717,16 @@ using namespace tp;
 static int check_cov_args(tp_ctx* ctx, int cosmo, int term, int geom, int precision) {
   if (!ctx) return TP_ERR_ARG;
   if (cosmo < 0 || cosmo >= ctx->n_cosmo) return tp_fail(ctx, TP_ERR_STATE, "no such cosmology");
-  if (term != 1 && term != 2 && term != 4) return tp_fail(ctx, TP_ERR_ARG, "term must be 1, 2 or 4");
+  if (term != 1 && term != 2 && (term < 4 || term > 7)) return tp_fail(ctx, TP_ERR_ARG, "term must be 1, 2, 4, 5, 6 or 7");
   if (geom < TP_GEOM_CIRCLE || geom > TP_GEOM_RECTANGLE) return tp_fail(ctx, TP_ERR_ARG, "unknown geometry");
   // the reference's T4 throws for every geometry but the infinite one (apertureStatisticsCovariance.cu:1183-1195)
   if (term == 4 && geom != TP_GEOM_INFINITE)
     return tp_fail(ctx, TP_ERR_ARG, "T4: only coded for the infinite survey geometry");
+  // T5 and T7 likewise (:1227-1230, :1310-1313); T6 for the square and the rectangle (:1235-1238)
+  if ((term == 5 || term == 7) && geom != TP_GEOM_INFINITE)
+    return tp_fail(ctx, TP_ERR_ARG, "T5/T7: only coded for the infinite survey geometry");
+  if (term == 6 && geom == TP_GEOM_CIRCLE)
+    return tp_fail(ctx, TP_ERR_ARG, "T6: only coded for square and rectangular survey geometries");
   if (geom == TP_GEOM_RECTANGLE && !(ctx->theta_max_smaller > 0))
     return tp_fail(ctx, TP_ERR_STATE, "rectangular geometry needs tp_set_rectangle_side");
   if (precision != TP_FP64 && precision != TP_FP32) return TP_ERR_ARG;
@@ -766,6 +741,10 @@ extern "C" int tp_cov_term_batch(tp_ctx* ctx, int cosmo, int term, int geometry,
   if (!th6 || !out || n < 0) return TP_ERR_ARG;
   for (int i = 0; i < 6 * n; ++i)
     if (!(th6[i] > 0)) return tp_fail(ctx, TP_ERR_ARG, "aperture radii must be > 0");
+  if (term == 6 && geometry == TP_GEOM_INFINITE)
+    return tp_fail(ctx, TP_ERR_ARG, "T6: only coded for square and rectangular survey geometries");
+  // the halo-model terms are evaluated in FP64 for either precision
+  if (term >= 5) precision = TP_FP64;
   cudaSetDevice(ctx->device);
   std::vector<std::array<double, 6>> v(n);
   for (int i = 0; i < n; ++i)
@@ -790,6 +769,7 @@ extern "C" int tp_cov_total_batch(tp_ctx* ctx, int cosmo, int term, int geometry
   if (!th123 || !th456 || !out || n < 0) return TP_ERR_ARG;
   for (int i = 0; i < 3 * n; ++i)
     if (!(th123[i] > 0) || !(th456[i] > 0)) return tp_fail(ctx, TP_ERR_ARG, "aperture radii must be > 0");
+  if (term >= 5) precision = TP_FP64;  // the halo-model terms are evaluated in FP64
   cudaSetDevice(ctx->device);
   std::vector<std::array<double, 6>> all;
   std::vector<std::vector<std::pair<int, int>>> use(n);  // (multiplicity, index into all)
@@ -797,8 +777,14 @@ extern "C" int tp_cov_total_batch(tp_ctx* ctx, int cosmo, int term, int geometry
   for (int i = 0; i < n; ++i) {
     const double* a = th123 + 3 * i;
     const double* b = th456 + 3 * i;
-    if (term == 2 && geometry == TP_GEOM_INFINITE) continue;
-    std::vector<PermTerm> terms = term == 1 ? t1_terms(a, b) : term == 2 ? t2_terms(a, b) : t4_terms(a, b);
+    // T2_total and T6_total are 0 for the infinite survey (:330-331, :849-850)
+    if ((term == 2 || term == 6) && geometry == TP_GEOM_INFINITE) continue;
+    std::vector<PermTerm> terms = term == 1   ? t1_terms(a, b)
+                                  : term == 2 ? t2_terms(a, b)
+                                  : term == 4 ? t4_terms(a, b)
+                                  : term == 5 ? t5_terms(a, b)
+                                  : term == 6 ? t6_terms(a, b)
+                                              : t7_terms(a, b);
     const double src[6] = {a[0], a[1], a[2], b[0], b[1], b[2]};
     for (const PermTerm& t : terms) {
       std::array<double, 6> th;

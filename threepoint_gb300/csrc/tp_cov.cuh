@@ -1,0 +1,134 @@
+// Shared pieces of the covariance integrals (tp_cov.cu: T1, T2, T4;
+// tp_halo.cu: the halo-model terms T5, T6, T7): the P_kappa node term, the
+// survey windows, the integral job list and the persistent engine launch.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <map>
+#include <vector>
+
+#include "tp_bispec.cuh"
+#include "tp_capi_internal.h"
+#include "tp_cubature.cuh"
+#include "tp_internal.cuh"
+
+namespace tp {
+
+// P_kappa line-of-sight term of node j at ell (bispectrum.cu:531-600,951-991):
+// W_j * T17(k) * P_nl(k, z_j), k = ell / f_K(z_j).
+template <typename R>
+__device__ __forceinline__ R pell_node(const R* __restrict__ hc, int j, R ell, R l2ell, const CosmoK<R>& K) {
+  typedef Mth<R> M;
+  const R W = hc[HC_W * NNODE + j];
+  if (W == (R)0) return (R)0;
+  const R k = ell * hc[HC_INVFK * NNODE + j];
+  const R l2k = l2ell + hc[HC_L2INVFK * NNODE + j];
+  const R P = plin<R>(K, k * K.h, l2k + K.l2h);
+  const R k3 = k * k * k;
+  const R pl = P * hc[HC_D1SQ * NNODE + j] * k3 * (R)(1.0 / (2 * PI * PI));
+  const R l2y = l2k + hc[HC_L2RS * NNODE + j];
+  const R y = k * hc[HC_RS * NNODE + j];
+  const R ysq = y * y;
+  R ph = hc[HC_A * NNODE + j] * M::ex2((R)3 * hc[HC_F1 * NNODE + j] * l2y) *
+         M::rcp((R)1 + hc[HC_B * NNODE + j] * M::ex2(hc[HC_F2 * NNODE + j] * l2y) +
+                M::ex2(((R)3 - hc[HC_GAM * NNODE + j]) * (hc[HC_L2F3C * NNODE + j] + l2y)));
+  ph = ph * ysq * M::rcp(ysq + hc[HC_XNU * NNODE + j]);
+  const R pq = pl * M::ex2(hc[HC_BETA * NNODE + j] * M::lg2((R)1 + pl)) * M::rcp((R)1 + pl * hc[HC_ALPHA * NNODE + j]) *
+               M::ex2(-(y * (R)0.25 + ysq * (R)0.125) * (R)1.4426950408889634);
+  const R pnl = (R)(2 * PI * PI) * (pq + ph) * M::rcp(k3);
+  // T17 correction (bispectrum.cu:971-979)
+  const R a1 = (R)1.3063, a2 = (R)1.1475, a3 = (R)0.62793, c1 = (R)9.5171e-4, c2 = (R)5.1543e-3;
+  const R corr = M::ex2(a1 * M::lg2((R)1 + c1 * M::ex2(-a1 * l2k)) - a3 * M::lg2((R)1 + c2 * M::ex2(-a2 * l2k)));
+  return W * corr * pnl;
+}
+
+// windows of the survey geometries (apertureStatisticsCovariance.cu:117-153)
+// G_square is the rectangle with two equal sides; G_rectangle (:154-172) has
+// side thetaMax along lx and thetaMax_smaller along ly
+template <typename R>
+__device__ inline R g_square(R thetaMax, R thetaMaxY, R lx, R ly) {
+  R t1 = (R)0.5 * lx * thetaMax, t2 = (R)0.5 * ly * thetaMaxY;
+  R j1 = fabs(t1) <= (R)1e-6 ? (R)1 : sin(t1) / t1;
+  R j2 = fabs(t2) <= (R)1e-6 ? (R)1 : sin(t2) / t2;
+  return j1 * j1 * j2 * j2;
+}
+template <typename R>
+__device__ inline R g_circle(R thetaMax, R ell) {
+  R t = thetaMax * ell;
+  R r = j1(t);
+  return r * r * (R)4 / (t * t);
+}
+
+struct CovJob {
+  double th[6];
+  double lmin, lmax;
+};
+
+// distinct integrals of one kind
+struct JobSet {
+  std::vector<CovJob> jobs;
+  std::map<std::vector<double>, int> index;
+  int add(const double* th, int nth, double lmin, double lmax) {
+    std::vector<double> key(th, th + nth);
+    key.push_back(lmin);
+    key.push_back(lmax);
+    auto it = index.find(key);
+    if (it != index.end()) return it->second;
+    CovJob j;
+    memset(&j, 0, sizeof(j));
+    for (int i = 0; i < nth; ++i) j.th[i] = th[i];
+    j.lmin = lmin;
+    j.lmax = lmax;
+    int id = (int)jobs.size();
+    jobs.push_back(j);
+    index[key] = id;
+    return id;
+  }
+};
+
+// Runs the adaptive engine over njobs integrals of policy P (one CTA per
+// integral, persistent grid), each to relative tolerance rel_tol in the L1 norm.
+template <int DIM, class P, int NT>
+__global__ void __launch_bounds__(NT) k_cov(P pol_in, int njobs, int* job_counter, EngineCfg cfg, char* scratch,
+                                            size_t slot_bytes) {
+  P pol = pol_in;
+  pol.loaded = 0;
+  adaptive_body<DIM, 1, NT, P>(pol, njobs, job_counter, cfg, scratch, slot_bytes);
+}
+
+template <int DIM, class P>
+inline int run_engine(tp_ctx* ctx, const P& pol, int njobs, double rel_tol) {
+  constexpr int NT = 256;
+  if (njobs == 0) return TP_OK;
+  size_t smem = engine_smem_bytes<DIM, 1, P>();
+  cudaError_t e = cudaFuncSetAttribute(k_cov<DIM, P, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return tp_cuda(ctx, e, "cov attribute");
+  int sms = 0, per_sm = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cov<DIM, P, NT>, NT, smem);
+  if (e != cudaSuccess || per_sm < 1) return tp_cuda(ctx, e ? e : cudaErrorInvalidConfiguration, "cov occupancy");
+  int grid = sms * per_sm;
+  if (ctx->max_ctas > 0 && grid > ctx->max_ctas) grid = ctx->max_ctas;
+  if (grid > njobs) grid = njobs;
+  // covariance integrals (6-D square-window T1, oscillating 2-D T2) refine to
+  // 10^5 regions and more: at least 2^19 regions per integral, with the grid
+  // trimmed so that the region stores stay within 64 GB of HBM
+  const int cap = std::max(ctx->region_cap, 1 << 19);
+  size_t slot = Slot<DIM, 1>::bytes(cap);
+  const size_t budget = size_t(64) << 30;
+  if ((size_t)grid * slot > budget) grid = std::max(1, (int)(budget / slot));
+  int st = ctx->ensure_scratch((size_t)grid * slot);
+  if (st) return st;
+  EngineCfg cfg{0.0, rel_tol, TP_NORM_L1, cap, 4000};
+  e = cudaMemsetAsync(ctx->d_counter, 0, sizeof(int), ctx->stream);
+  if (e == cudaSuccess) {
+    k_cov<DIM, P, NT><<<grid, NT, smem, ctx->stream>>>(pol, njobs, ctx->d_counter, cfg, ctx->d_scratch, slot);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+  return tp_cuda(ctx, e, "cov launch");
+}
+
+}  // namespace tp

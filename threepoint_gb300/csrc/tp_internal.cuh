@@ -129,6 +129,32 @@ enum HaloCoef {
   HC_COUNT
 };
 
+// Halo model of the covariance terms T5, T6, T7 (cuda_version/halomodel.cu).
+constexpr int NM = 128;                          // mass bins of the sigma^2(m) tables (n_mbins)
+constexpr double LOGM_MIN = 9.0, LOGM_MAX = 17.0;  // log10(M / (Msun/h)) range
+constexpr double RHO_CRIT = 2.7754e11;           // critical density [Msun h^2 / Mpc^3]
+
+// Per-node rows of the halo-model line-of-sight integrals (z-only parts of
+// trispectrum_integrand / pentaspectrum_integrand at the 96 fixed nodes, in
+// the node order of the other node tables). The halo model reads f_K, g and
+// D1 by linear interpolation on the grid z_i = i z_max / 255
+// (halomodel.cu:300-311,398-408), not by the mid-bin rule of b_kappa.
+enum HaloNodeRow {
+  HN_INVCHI = 0,  // 1 / f_K(z)
+  HN_D1SQ,        // D1(z)^2
+  HN_DC2,         // delta_c(z)^2, delta_c = 1.686 (1 + 0.0123 log10 Om(z))
+  HN_CZ,          // (1 + z)^-1.01 (redshift part of the Duffy et al. concentration)
+  HN_WTRI,        // gauss w dz/2 g^4 / f_K^2 (c/H0) / E (1.5 Om (H0/c)^2)^4 (1+z)^4
+  HN_WPEN,        // gauss w dz/2 g^6 / f_K^4 (c/H0) / E (1.5 Om (H0/c)^2)^6 (1+z)^6
+  HN_COUNT
+};
+
+// Halo-model tables of one cosmology: sigma^2(m_i) and dsigma^2/dm(m_i) at
+// z = 0 for m_i = 10^(LOGM_MIN + i (LOGM_MAX - LOGM_MIN) / NM), and the node rows.
+struct HaloTab {
+  double sig2[NM], dsig2[NM];
+  double hn[HN_COUNT * NNODE];
+};
 
 // ---- helpers shared by several translation units ---------------------------
 __host__ __device__ inline double eh_linear_pk(const EHConst& e, double k) {

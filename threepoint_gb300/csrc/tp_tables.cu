@@ -627,6 +627,48 @@ TP_TABLE_KERNEL k_node_coefs(const CosmoDev* cos, const TablesDev* tab, double* 
   }
 }
 
+// Halo-model node rows (trispectrum_integrand / pentaspectrum_integrand,
+// halomodel.cu:392-496, their z-only factors) at the 96 line-of-sight nodes.
+__global__ void k_halo_nodes(const CosmoDev* cos, const TablesDev* tab, int ci, HaloTab* halo) {
+  const int j = threadIdx.x;
+  if (j >= NNODE) return;
+  const CosmoDev c = cos[ci];
+  const TablesDev& t = tab[ci];
+  const int i = j >> 1;
+  const double cx = c.zmax / 2, dx = c.zmax / 2;
+  const double z = (j & 1) ? cx + dx * c_gq_a[i] : cx - dx * c_gq_a[i];
+  const double wq = c_gq_w[i] * dx;
+  // linear interpolation on z_i = i z_max / (NZ - 1) (halomodel.cu:300-311)
+  double f = z / c.zmax * (NZ - 1);
+  int idx = (int)f;
+  f -= idx;
+  if (idx == NZ - 1) {
+    idx = NZ - 2;
+    f = 1.;
+  }
+  const double g = t.g[idx] * (1 - f) + t.g[idx + 1] * f;
+  const double chi = t.f_K[idx] * (1 - f) + t.f_K[idx + 1] * f;
+  const double D1 = t.D1[idx] * (1 - f) + t.D1[idx + 1] * f;
+  const double aa = 1. / (1 + z);
+  const double omz = c.om / (c.om + aa * (aa * aa * c.ow + (1. - c.om - c.ow)));  // om_m_of_z, bispectrum.cu:439-447
+  const double dc = 1.686 * (1 + 0.0123 * log10(omz));
+  const double pre = 1.5 * c.om / C_OVER_H0 / C_OVER_H0;
+  const double los = wq * C_OVER_H0 / d_E(c, z);
+  const double g2 = g * g, pre2 = pre * pre, zp2 = (1 + z) * (1 + z);
+  double* h = halo->hn;
+  h[HN_INVCHI * NNODE + j] = 1. / chi;
+  h[HN_D1SQ * NNODE + j] = D1 * D1;
+  h[HN_DC2 * NNODE + j] = dc * dc;
+  h[HN_CZ * NNODE + j] = pow(1 + z, -1.01);
+  h[HN_WTRI * NNODE + j] = los * g2 * g2 / (chi * chi) * pre2 * pre2 * zp2 * zp2;
+  h[HN_WPEN * NNODE + j] = los * g2 * g2 * g2 / (chi * chi * chi * chi) * pre2 * pre2 * pre2 * zp2 * zp2 * zp2;
+}
+
+cudaError_t build_halo_nodes(const CosmoDev* d_cos, const TablesDev* d_tab, int ci, HaloTab* d_halo, cudaStream_t s) {
+  k_halo_nodes<<<1, NNODE, 0, s>>>(d_cos, d_tab, ci, d_halo);
+  return cudaGetLastError();
+}
+
 // Normalise the LOS weights of the FP32 node table by their maximum (kept in
 // wscale) so that FP32 products stay far from the float range limits, and
 // build the integrand constant blocks.

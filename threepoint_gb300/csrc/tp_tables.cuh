@@ -18,4 +18,8 @@ cudaError_t build_tables(const CosmoDev* d_cos, EHConst* d_eh, const double* d_n
                          double* d_wscale32, CosmoK<double>* d_ck64, CosmoK<float>* d_ck32, float4* d_plt,
                          double* d_ehg, int n, cudaStream_t s);
 
+// Fills the node rows (HN_*) of the halo-model tables of cosmology ci on
+// stream s from its z-tables (launches one small kernel).
+cudaError_t build_halo_nodes(const CosmoDev* d_cos, const TablesDev* d_tab, int ci, HaloTab* d_halo, cudaStream_t s);
+
 }  // namespace tp
