@@ -335,7 +335,8 @@ int tp_ogata_weights(double* out);
  * out[i] = T_term(th123[i], th456[i]). T5 and T7 exist for the infinite
  * geometry only, T6 for the square and the rectangle (0 for the infinite
  * geometry, as T6_total returns); the others are TP_ERR_ARG, where the
- * reference throws. T5-T7 are evaluated in FP64 whatever precision asks. */
+ * reference throws. precision TP_FP64 is the reference's arithmetic; with
+ * TP_FP32 the line-of-sight node sums run in FP32 (the cubature stays FP64). */
 int tp_cov_total_batch(tp_ctx* ctx, int cosmo_index, int term, int geometry, double theta_max, double area,
                        const double* th123, const double* th456, int n, int precision, double* out,
                        int* n_capped);
@@ -368,9 +369,9 @@ int tp_ctx_set_cov_tolerance(tp_ctx* ctx, int term, double rel_tol);
  *   integrand_T6_square / _rectangle, integrand_T7_infinite, :2151-2314),
  *   before the 1/area/(2 pi)^n factors. */
 int tp_halo_tables(tp_ctx* ctx, int cosmo_index, double* out);
-int tp_halo_los(tp_ctx* ctx, int cosmo_index, const double* pts, long n, double* tri, double* penta);
+int tp_halo_los(tp_ctx* ctx, int cosmo_index, const double* pts, long n, int precision, double* tri, double* penta);
 int tp_halo_integrand_points(tp_ctx* ctx, int cosmo_index, int term, int geometry, double theta_max,
-                             const double* th6, const double* x, long n, double* out);
+                             const double* th6, const double* x, long n, int precision, double* out);
 
 /* ---- likelihood of <Map^3> model vectors -------------------------------- */
 

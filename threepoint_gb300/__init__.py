@@ -183,8 +183,8 @@ def lib():
         L.tp_cov_term_batch.argtypes = [p, i, i, i, d, d, dp, i, i, dp, ip]
         L.tp_set_rectangle_side.argtypes = [p, d]
         L.tp_halo_tables.argtypes = [p, i, dp]
-        L.tp_halo_los.argtypes = [p, i, dp, l, dp, dp]
-        L.tp_halo_integrand_points.argtypes = [p, i, i, i, d, dp, dp, l, dp]
+        L.tp_halo_los.argtypes = [p, i, dp, l, i, dp, dp]
+        L.tp_halo_integrand_points.argtypes = [p, i, i, i, d, dp, dp, l, i, dp]
         L.tp_ctx_set_cov_tolerance.argtypes = [p, i, d]
         L.tp_cov_params_from_file.argtypes = [C.c_char_p, C.POINTER(_CovParams)]
         L.tp_gamma_config_from_file.argtypes = [C.c_char_p, C.POINTER(_GammaConfig)]
@@ -476,8 +476,7 @@ class Context:
         """T1_total / T2_total / T4_total / T5_total / T6_total / T7_total for
         pairs of triplets (apertureStatisticsCovariance.cu:272-1044). With
         check=False an integral that hit its region or sweep cap does not
-        raise; the number of such integrals is left in self.last_capped. The
-        halo-model terms 5-7 are evaluated in FP64 for either precision."""
+        raise; the number of such integrals is left in self.last_capped."""
         a = _arr(th123).reshape(-1, 3)
         b = _arr(th456).reshape(-1, 3)
         out = np.zeros(len(a))
@@ -529,15 +528,15 @@ class Context:
         _check(self._h, lib().tp_halo_tables(self._h, cosmo_index, _dp(out)))
         return out[:128].copy(), out[128:].copy()
 
-    def halo_los(self, pts, cosmo_index=0):
+    def halo_los(self, pts, cosmo_index=0, precision=FP64):
         """One-halo line-of-sight trispectrum (l1..l4) and pentaspectrum
         (l1..l6) at rows (m, l1, ..., l6)."""
         pts = _arr(pts).reshape(-1, 7)
         tri, pen = np.zeros(len(pts)), np.zeros(len(pts))
-        _check(self._h, lib().tp_halo_los(self._h, cosmo_index, _dp(pts), len(pts), _dp(tri), _dp(pen)))
+        _check(self._h, lib().tp_halo_los(self._h, cosmo_index, _dp(pts), len(pts), precision, _dp(tri), _dp(pen)))
         return tri, pen
 
-    def halo_integrand(self, term, th6, x, geometry=GEOM_INFINITE, thetaMax=0.0, cosmo_index=0):
+    def halo_integrand(self, term, th6, x, geometry=GEOM_INFINITE, thetaMax=0.0, cosmo_index=0, precision=FP64):
         """Integrand of T5 (rows of 6) / T6, T7 (rows of 7) at points x, before
         the 1/area/(2 pi)^n normalisation."""
         nd = 6 if term == 5 else 7
@@ -545,7 +544,7 @@ class Context:
         th = _arr(th6)
         out = np.zeros(len(x))
         _check(self._h, lib().tp_halo_integrand_points(self._h, cosmo_index, term, geometry, thetaMax, _dp(th),
-                                                        _dp(x), len(x), _dp(out)))
+                                                        _dp(x), len(x), precision, _dp(out)))
         return out
 
 

@@ -651,7 +651,7 @@ static int cov_terms(tp_ctx* ctx, int cosmo, int term, int geom, double theta_ma
   }
   if (term >= 5) {
     if (term != 6 && !(area > 0)) return tp_fail(ctx, TP_ERR_ARG, "T5 and T7 need area > 0");
-    int st = halo_terms(ctx, cosmo, term, geom, theta_max, area, th6, out, bad);
+    int st = halo_terms(ctx, cosmo, term, geom, theta_max, area, th6, sizeof(R) == 4 ? TP_FP32 : TP_FP64, out, bad);
     if (st || term != 6) return st;
     // T6 = (1-D integral over ell_1 of integrand_T2_part1 with (theta1,
     // theta2) on [1e-4, lMax], :1247-1255) x its 7-D halo integral; the
@@ -743,8 +743,6 @@ extern "C" int tp_cov_term_batch(tp_ctx* ctx, int cosmo, int term, int geometry,
     if (!(th6[i] > 0)) return tp_fail(ctx, TP_ERR_ARG, "aperture radii must be > 0");
   if (term == 6 && geometry == TP_GEOM_INFINITE)
     return tp_fail(ctx, TP_ERR_ARG, "T6: only coded for square and rectangular survey geometries");
-  // the halo-model terms are evaluated in FP64 for either precision
-  if (term >= 5) precision = TP_FP64;
   cudaSetDevice(ctx->device);
   std::vector<std::array<double, 6>> v(n);
   for (int i = 0; i < n; ++i)
@@ -769,7 +767,6 @@ extern "C" int tp_cov_total_batch(tp_ctx* ctx, int cosmo, int term, int geometry
   if (!th123 || !th456 || !out || n < 0) return TP_ERR_ARG;
   for (int i = 0; i < 3 * n; ++i)
     if (!(th123[i] > 0) || !(th456[i] > 0)) return tp_fail(ctx, TP_ERR_ARG, "aperture radii must be > 0");
-  if (term >= 5) precision = TP_FP64;  // the halo-model terms are evaluated in FP64
   cudaSetDevice(ctx->device);
   std::vector<std::array<double, 6>> all;
   std::vector<std::vector<std::pair<int, int>>> use(n);  // (multiplicity, index into all)

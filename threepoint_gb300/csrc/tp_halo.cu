@@ -83,6 +83,27 @@ struct SigmaPol {
   }
 };
 
+// FP32 copy of the node rows, the two weight rows scaled by their maximum
+__global__ void k_halo_rows_f32(HaloTab* t) {
+  const int j = threadIdx.x;
+  if (j >= NNODE) return;
+  double wmax[2] = {0, 0};
+  for (int k = 0; k < NNODE; ++k) {
+    wmax[0] = fmax(wmax[0], fabs(t->hn[HN_WTRI * NNODE + k]));
+    wmax[1] = fmax(wmax[1], fabs(t->hn[HN_WPEN * NNODE + k]));
+  }
+  for (int r = 0; r < HN_COUNT; ++r) {
+    double v = t->hn[r * NNODE + j];
+    if (r == HN_WTRI) v /= wmax[0];
+    if (r == HN_WPEN) v /= wmax[1];
+    t->hnf[r * NNODE + j] = (float)v;
+  }
+  if (j == 0) {
+    t->wmax[0] = wmax[0];
+    t->wmax[1] = wmax[1];
+  }
+}
+
 __global__ void k_halo_copy_tables(const double* src, HaloTab* dst) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < NM) {
@@ -105,47 +126,75 @@ __device__ __forceinline__ R horner(const R* c, int n, R y) {
   return s;
 }
 
+#define TP_SICI_SA                                                                                               \
+  1, -4.54393409816329991e-2, 1.15457225751016682e-3, -1.41018536821330254e-5, 9.43280809438713025e-8,           \
+      -3.53201978997168357e-10, 7.08240282274875911e-13, -6.05338212010422477e-16
+#define TP_SICI_SB                                                                                              \
+  1, 1.01162145739225565e-2, 4.99175116169755106e-5, 1.55654986308745614e-7, 3.28067571055789734e-10,          \
+      4.5049097575386581e-13, 3.21107051193712168e-16
+#define TP_SICI_CA                                                                                              \
+  -0.25, 7.51851524438898291e-3, -1.27528342240267686e-4, 1.05297363846239184e-6, -4.68889508144848019e-9,      \
+      1.06480802891189243e-11, -9.93728488857585407e-15
+#define TP_SICI_CB                                                                                              \
+  1, 1.1592605689110735e-2, 6.72126800814254432e-5, 2.55533277086129636e-7, 6.97071295760958946e-10,            \
+      1.38536352772778619e-12, 1.89106054713059759e-15, 1.39759616731376855e-18
+#define TP_SICI_FA                                                                                              \
+  1, 7.44437068161936700618e2, 1.96396372895146869801e5, 2.37750310125431834034e7, 1.43073403821274636888e9,    \
+      4.33736238870432522765e10, 6.40533830574022022911e11, 4.20968180571076940208e12, 1.00795182980368574617e13, \
+      4.94816688199951963482e12, -4.94701168645415959931e11
+#define TP_SICI_FB                                                                                              \
+  1, 7.46437068161927678031e2, 1.97865247031583951450e5, 2.41535670165126845144e7, 1.47478952192985464958e9,    \
+      4.58595115847765779830e10, 7.08501308149515401563e11, 5.06084464593475076774e12, 1.43468549171581016479e13, \
+      1.11535493509914254097e13
+#define TP_SICI_GA                                                                                              \
+  1, 8.1359520115168615e2, 2.35239181626478200e5, 3.12557570795778731e7, 2.06297595146763354e9,                 \
+      6.83052205423625007e10, 1.09049528450362786e12, 7.57664583257834349e12, 1.81004487464664575e13,           \
+      6.43291613143049485e12, -1.36517137670871689e12
+#define TP_SICI_GB                                                                                              \
+  1, 8.19595201151451564e2, 2.40036752835578777e5, 3.26026661647090822e7, 2.23355543278099360e9,                \
+      7.87465017341829930e10, 1.39866710696414565e12, 1.17164723371736605e13, 4.01839087307656620e13,           \
+      3.99653257887490811e13
+
+template <typename R>
 struct SiCiCoef {
   // x < 4
-  double sa[8], sb[7], ca[7], cb[8];
+  R sa[8], sb[7], ca[7], cb[8];
   // x >= 4
-  double fa[11], fb[10], ga[11], gb[10];
+  R fa[11], fb[10], ga[11], gb[10];
 };
-__constant__ SiCiCoef c_sici = {
-    {1, -4.54393409816329991e-2, 1.15457225751016682e-3, -1.41018536821330254e-5, 9.43280809438713025e-8,
-     -3.53201978997168357e-10, 7.08240282274875911e-13, -6.05338212010422477e-16},
-    {1, 1.01162145739225565e-2, 4.99175116169755106e-5, 1.55654986308745614e-7, 3.28067571055789734e-10,
-     4.5049097575386581e-13, 3.21107051193712168e-16},
-    {-0.25, 7.51851524438898291e-3, -1.27528342240267686e-4, 1.05297363846239184e-6, -4.68889508144848019e-9,
-     1.06480802891189243e-11, -9.93728488857585407e-15},
-    {1, 1.1592605689110735e-2, 6.72126800814254432e-5, 2.55533277086129636e-7, 6.97071295760958946e-10,
-     1.38536352772778619e-12, 1.89106054713059759e-15, 1.39759616731376855e-18},
-    {1, 7.44437068161936700618e2, 1.96396372895146869801e5, 2.37750310125431834034e7, 1.43073403821274636888e9,
-     4.33736238870432522765e10, 6.40533830574022022911e11, 4.20968180571076940208e12, 1.00795182980368574617e13,
-     4.94816688199951963482e12, -4.94701168645415959931e11},
-    {1, 7.46437068161927678031e2, 1.97865247031583951450e5, 2.41535670165126845144e7, 1.47478952192985464958e9,
-     4.58595115847765779830e10, 7.08501308149515401563e11, 5.06084464593475076774e12, 1.43468549171581016479e13,
-     1.11535493509914254097e13},
-    {1, 8.1359520115168615e2, 2.35239181626478200e5, 3.12557570795778731e7, 2.06297595146763354e9,
-     6.83052205423625007e10, 1.09049528450362786e12, 7.57664583257834349e12, 1.81004487464664575e13,
-     6.43291613143049485e12, -1.36517137670871689e12},
-    {1, 8.19595201151451564e2, 2.40036752835578777e5, 3.26026661647090822e7, 2.23355543278099360e9,
-     7.87465017341829930e10, 1.39866710696414565e12, 1.17164723371736605e13, 4.01839087307656620e13,
-     3.99653257887490811e13}};
+__constant__ SiCiCoef<double> c_sici = {{TP_SICI_SA}, {TP_SICI_SB}, {TP_SICI_CA}, {TP_SICI_CB},
+                                        {TP_SICI_FA}, {TP_SICI_FB}, {TP_SICI_GA}, {TP_SICI_GB}};
+__constant__ SiCiCoef<float> c_sicif = {{TP_SICI_SA}, {TP_SICI_SB}, {TP_SICI_CA}, {TP_SICI_CB},
+                                        {TP_SICI_FA}, {TP_SICI_FB}, {TP_SICI_GA}, {TP_SICI_GB}};
 
 constexpr double EULER_GAMMA = 0.5772156649;  // the value halomodel.cu:83 uses
 
+template <typename R>
+__device__ __forceinline__ const SiCiCoef<R>& sici_coef() {
+  if constexpr (sizeof(R) == 8) return c_sici;
+  else return c_sicif;
+}
+
 // Si(x) / x and (Ci(x) - gamma - ln x) / x^2 for x < 4
-__device__ __forceinline__ void sici_small(double x2, double& si_over_x, double& ci_rest_over_x2) {
-  si_over_x = horner(c_sici.sa, 8, x2) / horner(c_sici.sb, 7, x2);
-  ci_rest_over_x2 = horner(c_sici.ca, 7, x2) / horner(c_sici.cb, 8, x2);
+template <typename R>
+__device__ __forceinline__ void sici_small(R x2, R& si_over_x, R& ci_rest_over_x2) {
+  const SiCiCoef<R>& k = sici_coef<R>();
+  si_over_x = horner(k.sa, 8, x2) / horner(k.sb, 7, x2);
+  ci_rest_over_x2 = horner(k.ca, 7, x2) / horner(k.cb, 8, x2);
 }
 // f(x), g(x) for x >= 4
-__device__ __forceinline__ void sici_fg(double x, double& f, double& g) {
-  const double y = 1.0 / (x * x);
-  f = horner(c_sici.fa, 11, y) / (horner(c_sici.fb, 10, y) * x);
-  g = horner(c_sici.ga, 11, y) * y / horner(c_sici.gb, 10, y);
+template <typename R>
+__device__ __forceinline__ void sici_fg(R x, R& f, R& g) {
+  const SiCiCoef<R>& k = sici_coef<R>();
+  const R y = (R)1 / (x * x);
+  f = horner(k.fa, 11, y) / (horner(k.fb, 10, y) * x);
+  g = horner(k.ga, 11, y) * y / horner(k.gb, 10, y);
 }
+
+__device__ __forceinline__ void sincos_r(double x, double* s, double* c) { sincos(x, s, c); }
+__device__ __forceinline__ void sincos_r(float x, float* s, float* c) { sincosf(x, s, c); }
+__device__ __forceinline__ double log_r(double x) { return log(x); }
+__device__ __forceinline__ float log_r(float x) { return logf(x); }
 
 // Truncated NFW profile in Fourier space times F(c) = ln(1+c) - c/(1+c)
 // (u_NFW, halomodel.cu:121-140), with arg1 = k r_200 / c, arg2 = arg1 (1+c):
@@ -154,39 +203,43 @@ __device__ __forceinline__ void sici_fg(double x, double& f, double& g) {
 // Si(b) - Si(a) = (f_a cos a + g_a sin a) - (f_b cos b + g_b sin b); below 4 on
 // both sides Ci(b) - Ci(a) = ln(1+c) + b^2 r(b) - a^2 r(a); and
 // sin(arg1 c) = sin(arg2 - arg1) = sin(arg2) cos(arg1) - cos(arg2) sin(arg1).
-__device__ __forceinline__ double u_nfw_f(double a1, double opc, double lnopc) {
-  const double a2 = a1 * opc;
-  double s1, c1, s2, c2;
-  sincos(a1, &s1, &c1);
-  sincos(a2, &s2, &c2);
-  double dsi, dci;
-  if (a2 < 4.0) {
-    double q1, r1, q2, r2;
-    sici_small(a1 * a1, q1, r1);
-    sici_small(a2 * a2, q2, r2);
+// In FP32 this keeps u accurate to ~1e-6 where the reference's direct
+// differences of Si and Ci (each near pi/2 or 0 for large arguments) would
+// lose every digit.
+template <typename R>
+__device__ __forceinline__ R u_nfw_f(R a1, R opc, R lnopc) {
+  const R a2 = a1 * opc;
+  R s1, c1, s2, c2;
+  sincos_r(a1, &s1, &c1);
+  sincos_r(a2, &s2, &c2);
+  R dsi, dci;
+  if (a2 < (R)4) {
+    R q1, r1, q2, r2;
+    sici_small<R>(a1 * a1, q1, r1);
+    sici_small<R>(a2 * a2, q2, r2);
     dsi = a2 * q2 - a1 * q1;
     dci = lnopc + a2 * a2 * r2 - a1 * a1 * r1;
-  } else if (a1 < 4.0) {
-    double q1, r1, f2, g2;
-    sici_small(a1 * a1, q1, r1);
-    sici_fg(a2, f2, g2);
-    dsi = (0.5 * PI - f2 * c2 - g2 * s2) - a1 * q1;
-    dci = (f2 * s2 - g2 * c2) - (EULER_GAMMA + log(a1) + a1 * a1 * r1);
+  } else if (a1 < (R)4) {
+    R q1, r1, f2, g2;
+    sici_small<R>(a1 * a1, q1, r1);
+    sici_fg<R>(a2, f2, g2);
+    dsi = ((R)(0.5 * PI) - f2 * c2 - g2 * s2) - a1 * q1;
+    dci = (f2 * s2 - g2 * c2) - ((R)EULER_GAMMA + log_r(a1) + a1 * a1 * r1);
   } else {
-    double f1, g1, f2, g2;
-    sici_fg(a1, f1, g1);
-    sici_fg(a2, f2, g2);
+    R f1, g1, f2, g2;
+    sici_fg<R>(a1, f1, g1);
+    sici_fg<R>(a2, f2, g2);
     dsi = (f1 * c1 + g1 * s1) - (f2 * c2 + g2 * s2);
     dci = (f2 * s2 - g2 * c2) - (f1 * s1 - g1 * c1);
   }
-  const double s12 = s2 * c1 - c2 * s1;  // sin(a2 - a1)
+  const R s12 = s2 * c1 - c2 * s1;  // sin(a2 - a1)
   return s1 * dsi + c1 * dci - s12 / a2;
 }
 
 // ---------------------------------------------------------------------------
 // T5 (6-D: ln l1, ln l2, ln l5, phi1, phi2, m), T6 (7-D: ln l3, ln l4, ln l5,
 // phi3, phi4, phi5, m), T7 (7-D: ln l1, ln l2, ln l4, ln l5, phi1, phi2, m).
-template <int KIND>
+template <int KIND, typename R = double>
 struct HaloProd {
   static constexpr int DIM = KIND == 5 ? 6 : 7;
   static constexpr int NL = KIND == 7 ? 6 : 4;  // ell arguments of the tri-/pentaspectrum
@@ -197,24 +250,23 @@ struct HaloProd {
   __device__ static int slot(int g) { return KIND == 5 ? (g >= NCH ? 1 : 0) : 0; }
   static constexpr int CH = 2;
   struct Rec {
-    double l[NL];
-    double pm;    // -rhobar/m dsig2/sig2 A (m/rhobar)^n: the point's mass-function factor
-    double s2m;   // sigma^2(m) at z = 0
-    double cm;    // mass part of the concentration, 10.14 (m / 2e12)^-0.081
-    double r200;  // r_200(m)
+    R l[NL];
+    double pm;    // -rhobar/m dsig2/sig2 A (m/rhobar)^n (x the weight scale in FP32): the mass-function factor
+    R s2m;        // sigma^2(m) at z = 0
+    R cm;         // mass part of the concentration, 10.14 (m / 2e12)^-0.081
+    R r200;       // r_200(m)
     double wt;    // filter product, ell factors and window
-    double pell, pl2;  // T5: ell_1 and log2 ell_1 of P(ell_1)
+    R pell, pl2;  // T5: ell_1 and log2 ell_1 of P(ell_1)
     int valid, los;
   };
   static constexpr int REC = (int)sizeof(Rec);
   const int* job_order = nullptr;
-  static constexpr size_t PSMEM =
-      sizeof(double) * HN_COUNT * NNODE + (KIND == 5 ? sizeof(double) * HC_COUNT * NNODE : 0) + 64;
+  static constexpr size_t PSMEM = sizeof(R) * HN_COUNT * NNODE + (KIND == 5 ? sizeof(R) * HC_COUNT * NNODE : 0) + 64;
 
   const CovJob* jobs;
   const HaloTab* halo;     // this cosmology's halo tables (global)
-  const double* hcoef;     // T5: Halofit node rows of P(ell)
-  CosmoK<double> ck;
+  const R* hcoef;          // T5: Halofit node rows of P(ell)
+  CosmoK<R> ck;
   double rhobar;
   double psn;              // shape-noise power of P(ell)
   int constant_ps;
@@ -222,17 +274,18 @@ struct HaloProd {
   double norm;
   double* out;
   int* status;
-  double* s_hn;
-  double* s_hc;
+  R* s_hn;
+  R* s_hc;
   double th[6], lmax;
   int loaded;
 
   // node tables into shared memory (all threads of the CTA)
   __device__ void load_tables(char* psmem) {
-    s_hn = (double*)psmem;
+    s_hn = (R*)psmem;
     s_hc = s_hn + HN_COUNT * NNODE;
     __syncthreads();
-    for (int i = threadIdx.x; i < HN_COUNT * NNODE; i += blockDim.x) s_hn[i] = halo->hn[i];
+    const R* hn = sizeof(R) == 8 ? (const R*)(const void*)halo->hn : (const R*)(const void*)halo->hnf;
+    for (int i = threadIdx.x; i < HN_COUNT * NNODE; i += blockDim.x) s_hn[i] = hn[i];
     if (KIND == 5)
       for (int i = threadIdx.x; i < HC_COUNT * NNODE; i += blockDim.x) s_hc[i] = hcoef[i];
     __syncthreads();
@@ -245,9 +298,10 @@ struct HaloProd {
     double mn = mr * mr * mr * mr;
     if (NL == 6) mn *= mr * mr;
     r.pm = -rhobar / m * ds2m / s2m * 0.322 * mn;
-    r.s2m = s2m;
-    r.cm = 10.14 * pow(m / 2e12, -0.081);
-    r.r200 = pow(0.75 / PI * mr / 200, 1. / 3.);
+    if (sizeof(R) == 4) r.pm *= halo->wmax[NL == 6 ? 1 : 0];
+    r.s2m = (R)s2m;
+    r.cm = (R)(10.14 * pow(m / 2e12, -0.081));
+    r.r200 = (R)pow(0.75 / PI * mr / 200, 1. / 3.);
   }
 
   __device__ void begin_job(int job, char* psmem, double* xmin, double* xmax) {
@@ -307,9 +361,9 @@ struct HaloProd {
           const double lp = l1 * l2 * l5;
           wt = uhat(l1 * th[0]) * uhat(l2 * th[1]) * uhat(l3 * th[2]) * uhat(l1 * th[3]) * uhat(l5 * th[4]) *
                uhat(l6 * th[5]) * lp * lp;
-          r.l[0] = l2, r.l[1] = l3, r.l[2] = l5, r.l[3] = l6;
-          r.pell = l1;
-          r.pl2 = log2(l1);
+          r.l[0] = (R)l2, r.l[1] = (R)l3, r.l[2] = (R)l5, r.l[3] = (R)l6;
+          r.pell = (R)l1;
+          r.pl2 = (R)log2(l1);
           ok = true;
         }
       }
@@ -324,7 +378,7 @@ struct HaloProd {
         const double G = g_square<double>(thetaMax, thetaMaxY, l3 * cp, l3 * sp);
         const double lp = l3 * l4 * l5;
         wt = uhat(l3 * th[2]) * uhat(l4 * th[3]) * uhat(l5 * th[4]) * uhat(l6 * th[5]) * lp * lp * G;
-        r.l[0] = l3, r.l[1] = l4, r.l[2] = l5, r.l[3] = l6;
+        r.l[0] = (R)l3, r.l[1] = (R)l4, r.l[2] = (R)l5, r.l[3] = (R)l6;
         ok = true;
       }
     } else {
@@ -336,7 +390,7 @@ struct HaloProd {
         const double lp = l1 * l2 * l4 * l5;
         wt = uhat(l1 * th[0]) * uhat(l2 * th[1]) * uhat(l3 * th[2]) * uhat(l4 * th[3]) * uhat(l5 * th[4]) *
              uhat(l6 * th[5]) * lp * lp;
-        r.l[0] = l1, r.l[1] = l2, r.l[2] = l3, r.l[3] = l4, r.l[4] = l5, r.l[5] = l6;
+        r.l[0] = (R)l1, r.l[1] = (R)l2, r.l[2] = (R)l3, r.l[3] = (R)l4, r.l[4] = (R)l5, r.l[5] = (R)l6;
         ok = true;
       }
     }
@@ -348,42 +402,48 @@ struct HaloProd {
   }
 
   __device__ void group(const char* recp, int g, double* pv) {
+    typedef Mth<R> M;
     const Rec& r = *(const Rec*)recp;
     if (KIND == 5 && g < NCH) {
       // P(ell_1) node chunk
-      KSum<double> acc;
+      KSum<R> acc;
       if (r.los) {
         const int j0 = g * (NNODE / NCH);
         for (int j = j0; j < j0 + NNODE / NCH; ++j) {
-          double v = pell_node<double>(s_hc, j, r.pell, r.pl2, ck);
+          R v = pell_node<R>(s_hc, j, r.pell, r.pl2, ck);
           if (v != v) v = 0;
           acc.add(v);
         }
       }
-      pv[0] = acc.s;
+      pv[0] = (double)acc.s;
       return;
     }
     const int ch = KIND == 5 ? g - NCH : g;
     const int j0 = ch * (NNODE / NCH);
-    const double q = 0.707, p = 0.3;
-    KSum<double> acc;
+    const R q = (R)0.707, p = (R)0.3;
+    KSum<R> acc;
     for (int j = j0; j < j0 + NNODE / NCH; ++j) {
-      const double invchi = s_hn[HN_INVCHI * NNODE + j];
+      const R invchi = s_hn[HN_INVCHI * NNODE + j];
       // Sheth-Tormen multiplicity at nu = delta_c^2 / sigma^2(m, z)
-      const double qnu = q * s_hn[HN_DC2 * NNODE + j] / (r.s2m * s_hn[HN_D1SQ * NNODE + j]);
-      const double fnu = (1 + pow(qnu, -p)) * sqrt(qnu / (2 * PI)) * exp(-0.5 * qnu);
+      const R qnu = q * s_hn[HN_DC2 * NNODE + j] / (r.s2m * s_hn[HN_D1SQ * NNODE + j]);
+      R fnu;
+      if constexpr (sizeof(R) == 8)
+        fnu = (1 + pow(qnu, -p)) * sqrt(qnu / (2 * PI)) * exp(-0.5 * qnu);
+      else
+        fnu = (1.f + M::ex2(-p * M::lg2(qnu))) * sqrtf(qnu * (float)(0.5 / PI)) *
+              M::ex2(qnu * (float)(-0.5 / LN2));
       // NFW: concentration, F(c), scale k -> arg1 = k r_200 / c
-      const double c = r.cm * s_hn[HN_CZ * NNODE + j];
-      const double opc = 1 + c;
-      const double lnopc = log(opc);
-      const double F = lnopc - c / opc;
-      const double a = r.r200 / c * invchi;
-      double prod = fnu * s_hn[(NL == 6 ? HN_WPEN : HN_WTRI) * NNODE + j];
+      const R c = r.cm * s_hn[HN_CZ * NNODE + j];
+      const R opc = 1 + c;
+      const R lnopc = log_r(opc);
+      const R invF = (R)1 / (lnopc - c / opc);
+      const R a = r.r200 / c * invchi;
+      R prod = fnu * s_hn[(NL == 6 ? HN_WPEN : HN_WTRI) * NNODE + j];
 #pragma unroll
-      for (int i = 0; i < NL; ++i) prod *= u_nfw_f(r.l[i] * a, opc, lnopc) / F;
+      for (int i = 0; i < NL; ++i) prod *= u_nfw_f<R>(r.l[i] * a, opc, lnopc) * invF;
       acc.add(prod);
     }
-    pv[0] = acc.s;
+    pv[0] = (double)acc.s;
   }
 
   __device__ void finalize(const char* recp, const double* sum, double* fv) {
@@ -408,19 +468,20 @@ struct HaloProd {
 
 // Integrand values of term KIND at points x (ndim = DIM): setup, every node
 // chunk and the final product as the engine forms them, one thread per point.
-template <int KIND>
-__global__ void k_halo_points(HaloProd<KIND> pol, const double* x, long n, double* out) {
+template <int KIND, typename R>
+__global__ void k_halo_points(HaloProd<KIND, R> pol, const double* x, long n, double* out) {
   extern __shared__ __align__(16) char psmem[];
   pol.load_tables(psmem);
   const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  typename HaloProd<KIND>::Rec r;
+  typedef HaloProd<KIND, R> P;
+  typename P::Rec r;
   double s[2] = {0, 0}, f;
-  if (pol.setup(0, x + i * HaloProd<KIND>::DIM, (char*)&r))
-    for (int g = 0; g < HaloProd<KIND>::G; ++g) {
+  if (pol.setup(0, x + i * P::DIM, (char*)&r))
+    for (int g = 0; g < P::G; ++g) {
       double v;
       pol.group((const char*)&r, g, &v);
-      s[HaloProd<KIND>::slot(g)] += v;
+      s[P::slot(g)] += v;
     }
   pol.finalize((const char*)&r, s, &f);
   out[i] = f;
@@ -429,21 +490,23 @@ __global__ void k_halo_points(HaloProd<KIND> pol, const double* x, long n, doubl
 // One-halo line-of-sight trispectrum (l1..l4) and pentaspectrum (l1..l6) at
 // rows (m, l1, ..., l6): trispectrum_limber_integrated /
 // pentaspectrum_limber_integrated over [0, z_max] (halomodel.cu:430-510).
-__global__ void k_halo_los(HaloProd<6> tri, HaloProd<7> pen, const double* pts, long n, double* otri, double* open) {
+template <typename R>
+__global__ void k_halo_los(HaloProd<6, R> tri, HaloProd<7, R> pen, const double* pts, long n, double* otri,
+                           double* open) {
   extern __shared__ __align__(16) char psmem[];
   tri.load_tables(psmem);
   pen.s_hn = tri.s_hn;
   const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const double* p = pts + 7 * i;
-  HaloProd<6>::Rec rt;
-  HaloProd<7>::Rec rp;
+  typename HaloProd<6, R>::Rec rt;
+  typename HaloProd<7, R>::Rec rp;
   tri.set_mass(rt, p[0]);
   pen.set_mass(rp, p[0]);
-  for (int k = 0; k < 4; ++k) rt.l[k] = p[1 + k];
-  for (int k = 0; k < 6; ++k) rp.l[k] = p[1 + k];
+  for (int k = 0; k < 4; ++k) rt.l[k] = (R)p[1 + k];
+  for (int k = 0; k < 6; ++k) rp.l[k] = (R)p[1 + k];
   double st = 0, sp = 0;
-  for (int g = 0; g < HaloProd<6>::NCH; ++g) {
+  for (int g = 0; g < HaloProd<6, R>::NCH; ++g) {
     double v;
     tri.group((const char*)&rt, g, &v);
     st += v;
@@ -491,6 +554,10 @@ int ensure_halo(tp_ctx* ctx, int cosmo) {
   k_halo_copy_tables<<<1, NM, 0, ctx->stream>>>((const double*)b, tab);
   e = cudaGetLastError();
   if (e == cudaSuccess) e = build_halo_nodes(ctx->d_cos, ctx->d_tab, cosmo, tab, ctx->stream);
+  if (e == cudaSuccess) {
+    k_halo_rows_f32<<<1, NNODE, 0, ctx->stream>>>(tab);
+    e = cudaGetLastError();
+  }
   if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
   if (e != cudaSuccess) return tp_cuda(ctx, e, "halo tables");
   ctx->halo_ready[cosmo] = 1;
@@ -500,13 +567,14 @@ int ensure_halo(tp_ctx* ctx, int cosmo) {
 namespace {
 
 // policy parameters of cosmology cosmo (everything but the job list and outputs)
-template <int KIND>
-int halo_policy(tp_ctx* ctx, int cosmo, double theta_max, double theta_max_y, double norm, HaloProd<KIND>& pol) {
+template <int KIND, typename R>
+int halo_policy(tp_ctx* ctx, int cosmo, double theta_max, double theta_max_y, double norm, HaloProd<KIND, R>& pol) {
   memset(&pol, 0, sizeof(pol));
   pol.halo = ctx->d_halo + cosmo;
-  pol.hcoef = ctx->d_hcoef + (size_t)cosmo * HC_COUNT * NNODE;
-  cudaError_t e = cudaMemcpyAsync(&pol.ck, (const char*)ctx->d_ck64 + sizeof(CosmoK<double>) * cosmo,
-                                  sizeof(CosmoK<double>), cudaMemcpyDeviceToHost, ctx->stream);
+  pol.hcoef = (sizeof(R) == 8 ? (const R*)(const void*)ctx->d_hcoef : (const R*)(const void*)ctx->d_hcoef32) +
+              (size_t)cosmo * HC_COUNT * NNODE;
+  cudaError_t e = cudaMemcpyAsync(&pol.ck, (const char*)(sizeof(R) == 8 ? ctx->d_ck64 : ctx->d_ck32) + sizeof(CosmoK<R>) * cosmo,
+                                  sizeof(CosmoK<R>), cudaMemcpyDeviceToHost, ctx->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
   if (e != cudaSuccess) return tp_cuda(ctx, e, "halo term constants");
   pol.rhobar = RHO_CRIT * ctx->h_cos[cosmo].om;
@@ -518,7 +586,7 @@ int halo_policy(tp_ctx* ctx, int cosmo, double theta_max, double theta_max_y, do
   return TP_OK;
 }
 
-template <int KIND>
+template <int KIND, typename R>
 int run_halo_kind(tp_ctx* ctx, int cosmo, const JobSet& js, double theta_max, double theta_max_y, double norm,
                   double rel_tol, std::vector<double>& res, int& bad) {
   res.assign(js.jobs.size(), 0.0);
@@ -531,13 +599,13 @@ int run_halo_kind(tp_ctx* ctx, int cosmo, const JobSet& js, double theta_max, do
   char* b = ctx->d_io;
   cudaError_t e = cudaMemcpyAsync(b + o_j, js.jobs.data(), sizeof(CovJob) * n, cudaMemcpyHostToDevice, ctx->stream);
   if (e != cudaSuccess) return tp_cuda(ctx, e, "halo term upload");
-  HaloProd<KIND> pol;
-  st = halo_policy<KIND>(ctx, cosmo, theta_max, theta_max_y, norm, pol);
+  HaloProd<KIND, R> pol;
+  st = halo_policy<KIND, R>(ctx, cosmo, theta_max, theta_max_y, norm, pol);
   if (st) return st;
   pol.jobs = (const CovJob*)(b + o_j);
   pol.out = (double*)(b + o_o);
   pol.status = (int*)(b + o_s);
-  st = run_engine<HaloProd<KIND>::DIM>(ctx, pol, (int)n, rel_tol);
+  st = run_engine<HaloProd<KIND, R>::DIM>(ctx, pol, (int)n, rel_tol);
   if (st) return st;
   std::vector<int> hs(n);
   e = cudaMemcpy(res.data(), b + o_o, sizeof(double) * n, cudaMemcpyDeviceToHost);
@@ -555,8 +623,9 @@ double halo_tol(const tp_ctx* ctx, int term) {
 
 }  // namespace
 
-int halo_terms(tp_ctx* ctx, int cosmo, int term, int geom, double theta_max, double area,
-               const std::vector<std::array<double, 6>>& th6, std::vector<double>& out, int& bad) {
+template <typename R>
+static int halo_terms_t(tp_ctx* ctx, int cosmo, int term, int geom, double theta_max, double area,
+                        const std::vector<std::array<double, 6>>& th6, std::vector<double>& out, int& bad) {
   const size_t n = th6.size();
   out.assign(n, 0.0);
   if (n == 0) return TP_OK;
@@ -571,16 +640,22 @@ int halo_terms(tp_ctx* ctx, int cosmo, int term, int geom, double theta_max, dou
   }
   std::vector<double> r;
   if (term == 5) {
-    st = run_halo_kind<5>(ctx, cosmo, js, theta_max, theta_max, 1 / area / pow(two_pi, 5), halo_tol(ctx, 5), r, bad);
+    st = run_halo_kind<5, R>(ctx, cosmo, js, theta_max, theta_max, 1 / area / pow(two_pi, 5), halo_tol(ctx, 5), r, bad);
   } else if (term == 7) {
-    st = run_halo_kind<7>(ctx, cosmo, js, theta_max, theta_max, 1 / area / pow(two_pi, 6), halo_tol(ctx, 7), r, bad);
+    st = run_halo_kind<7, R>(ctx, cosmo, js, theta_max, theta_max, 1 / area / pow(two_pi, 6), halo_tol(ctx, 7), r, bad);
   } else {
     const double tmy = geom == TP_GEOM_RECTANGLE ? ctx->theta_max_smaller : theta_max;
-    st = run_halo_kind<6>(ctx, cosmo, js, theta_max, tmy, 1 / pow(two_pi, 6), halo_tol(ctx, 6), r, bad);
+    st = run_halo_kind<6, R>(ctx, cosmo, js, theta_max, tmy, 1 / pow(two_pi, 6), halo_tol(ctx, 6), r, bad);
   }
   if (st) return st;
   for (size_t i = 0; i < n; ++i) out[i] = r[id[i]];
   return TP_OK;
+}
+
+int halo_terms(tp_ctx* ctx, int cosmo, int term, int geom, double theta_max, double area,
+               const std::vector<std::array<double, 6>>& th6, int precision, std::vector<double>& out, int& bad) {
+  return precision == TP_FP32 ? halo_terms_t<float>(ctx, cosmo, term, geom, theta_max, area, th6, out, bad)
+                              : halo_terms_t<double>(ctx, cosmo, term, geom, theta_max, area, th6, out, bad);
 }
 
 double halo_lmax(int term, const double* t) {
@@ -608,8 +683,32 @@ extern "C" int tp_halo_tables(tp_ctx* ctx, int cosmo, double* out) {
   return tp_cuda(ctx, e, "halo tables");
 }
 
-extern "C" int tp_halo_los(tp_ctx* ctx, int cosmo, const double* pts, long n, double* tri, double* penta) {
-  if (!pts || !tri || !penta || n < 0) return TP_ERR_ARG;
+template <typename R>
+static int halo_los_t(tp_ctx* ctx, int cosmo, const double* pts, long n, double* tri, double* penta) {
+  HaloProd<6, R> tri_pol;
+  HaloProd<7, R> pen_pol;
+  int st = halo_policy<6, R>(ctx, cosmo, 0, 0, 1, tri_pol);
+  if (!st) st = halo_policy<7, R>(ctx, cosmo, 0, 0, 1, pen_pol);
+  if (st) return st;
+  const size_t o_t = (sizeof(double) * 7 * n + 255) & ~size_t(255), o_p = o_t + ((sizeof(double) * n + 255) & ~size_t(255));
+  st = ctx->ensure_io(o_p + sizeof(double) * n + 256);
+  if (st) return st;
+  char* b = ctx->d_io;
+  cudaError_t e = cudaMemcpyAsync(b, pts, sizeof(double) * 7 * n, cudaMemcpyHostToDevice, ctx->stream);
+  if (e == cudaSuccess) {
+    k_halo_los<R><<<(unsigned)((n + 63) / 64), 64, HaloProd<6, R>::PSMEM, ctx->stream>>>(
+        tri_pol, pen_pol, (const double*)b, n, (double*)(b + o_t), (double*)(b + o_p));
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpyAsync(tri, b + o_t, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(penta, b + o_p, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+  return tp_cuda(ctx, e, "halo line-of-sight points");
+}
+
+extern "C" int tp_halo_los(tp_ctx* ctx, int cosmo, const double* pts, long n, int precision, double* tri,
+                           double* penta) {
+  if (!pts || !tri || !penta || n < 0 || (precision != TP_FP64 && precision != TP_FP32)) return TP_ERR_ARG;
   int st = check_halo_args(ctx, cosmo);
   if (st) return st;
   if (n == 0) return TP_OK;
@@ -619,33 +718,17 @@ extern "C" int tp_halo_los(tp_ctx* ctx, int cosmo, const double* pts, long n, do
     for (int k = 1; k < 7; ++k)
       if (!(pts[7 * i + k] > 0)) return tp_fail(ctx, TP_ERR_ARG, "ell must be > 0");
   }
-  HaloProd<6> tri_pol;
-  HaloProd<7> pen_pol;
-  st = halo_policy<6>(ctx, cosmo, 0, 0, 1, tri_pol);
-  if (!st) st = halo_policy<7>(ctx, cosmo, 0, 0, 1, pen_pol);
-  if (st) return st;
-  const size_t o_t = (sizeof(double) * 7 * n + 255) & ~size_t(255), o_p = o_t + ((sizeof(double) * n + 255) & ~size_t(255));
-  st = ctx->ensure_io(o_p + sizeof(double) * n + 256);
-  if (st) return st;
-  char* b = ctx->d_io;
-  cudaError_t e = cudaMemcpyAsync(b, pts, sizeof(double) * 7 * n, cudaMemcpyHostToDevice, ctx->stream);
-  if (e == cudaSuccess) {
-    k_halo_los<<<(unsigned)((n + 63) / 64), 64, HaloProd<6>::PSMEM, ctx->stream>>>(tri_pol, pen_pol, (const double*)b, n,
-                                                                                (double*)(b + o_t), (double*)(b + o_p));
-    e = cudaGetLastError();
-  }
-  if (e == cudaSuccess) e = cudaMemcpyAsync(tri, b + o_t, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->stream);
-  if (e == cudaSuccess) e = cudaMemcpyAsync(penta, b + o_p, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->stream);
-  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
-  return tp_cuda(ctx, e, "halo line-of-sight points");
+  return precision == TP_FP32 ? halo_los_t<float>(ctx, cosmo, pts, n, tri, penta)
+                              : halo_los_t<double>(ctx, cosmo, pts, n, tri, penta);
 }
 
-template <int KIND>
+template <int KIND, typename R>
 static int halo_points(tp_ctx* ctx, int cosmo, const double* th6, double lmax, double theta_max, double theta_max_y,
                        const double* x, long n, double* out) {
-  constexpr int D = HaloProd<KIND>::DIM;
-  HaloProd<KIND> pol;
-  int st = halo_policy<KIND>(ctx, cosmo, theta_max, theta_max_y, 1, pol);
+  typedef HaloProd<KIND, R> P;
+  constexpr int D = P::DIM;
+  P pol;
+  int st = halo_policy<KIND, R>(ctx, cosmo, theta_max, theta_max_y, 1, pol);
   if (st) return st;
   for (int k = 0; k < 6; ++k) pol.th[k] = th6[k];
   pol.lmax = lmax;
@@ -655,8 +738,8 @@ static int halo_points(tp_ctx* ctx, int cosmo, const double* th6, double lmax, d
   char* b = ctx->d_io;
   cudaError_t e = cudaMemcpyAsync(b, x, sizeof(double) * D * n, cudaMemcpyHostToDevice, ctx->stream);
   if (e == cudaSuccess) {
-    k_halo_points<KIND><<<(unsigned)((n + 63) / 64), 64, HaloProd<KIND>::PSMEM, ctx->stream>>>(pol, (const double*)b, n,
-                                                                                             (double*)(b + o_o));
+    k_halo_points<KIND, R><<<(unsigned)((n + 63) / 64), 64, P::PSMEM, ctx->stream>>>(pol, (const double*)b, n,
+                                                                                   (double*)(b + o_o));
     e = cudaGetLastError();
   }
   if (e == cudaSuccess) e = cudaMemcpyAsync(out, b + o_o, sizeof(double) * n, cudaMemcpyDeviceToHost, ctx->stream);
@@ -664,9 +747,18 @@ static int halo_points(tp_ctx* ctx, int cosmo, const double* th6, double lmax, d
   return tp_cuda(ctx, e, "halo integrand points");
 }
 
+template <typename R>
+static int halo_points_t(tp_ctx* ctx, int cosmo, int term, const double* th6, double lmax, double tm, double tmy,
+                         const double* x, long n, double* out) {
+  if (term == 5) return halo_points<5, R>(ctx, cosmo, th6, lmax, tm, tmy, x, n, out);
+  if (term == 6) return halo_points<6, R>(ctx, cosmo, th6, lmax, tm, tmy, x, n, out);
+  return halo_points<7, R>(ctx, cosmo, th6, lmax, tm, tmy, x, n, out);
+}
+
 extern "C" int tp_halo_integrand_points(tp_ctx* ctx, int cosmo, int term, int geometry, double theta_max,
-                                        const double* th6, const double* x, long n, double* out) {
-  if (!th6 || !x || !out || n < 0 || term < 5 || term > 7) return TP_ERR_ARG;
+                                        const double* th6, const double* x, long n, int precision, double* out) {
+  if (!ctx || !th6 || !x || !out || n < 0 || term < 5 || term > 7) return TP_ERR_ARG;
+  if (precision != TP_FP64 && precision != TP_FP32) return TP_ERR_ARG;
   if (term == 6 && geometry != TP_GEOM_SQUARE && geometry != TP_GEOM_RECTANGLE)
     return tp_fail(ctx, TP_ERR_ARG, "T6: only coded for square and rectangular survey geometries");
   if (term == 6 && geometry == TP_GEOM_RECTANGLE && !(ctx->theta_max_smaller > 0))
@@ -681,9 +773,8 @@ extern "C" int tp_halo_integrand_points(tp_ctx* ctx, int cosmo, int term, int ge
   }
   const double lmax = halo_lmax(term, th6);
   const double tmy = geometry == TP_GEOM_RECTANGLE ? ctx->theta_max_smaller : theta_max;
-  if (term == 5) return halo_points<5>(ctx, cosmo, th6, lmax, theta_max, tmy, x, n, out);
-  if (term == 6) return halo_points<6>(ctx, cosmo, th6, lmax, theta_max, tmy, x, n, out);
-  return halo_points<7>(ctx, cosmo, th6, lmax, theta_max, tmy, x, n, out);
+  return precision == TP_FP32 ? halo_points_t<float>(ctx, cosmo, term, th6, lmax, theta_max, tmy, x, n, out)
+                              : halo_points_t<double>(ctx, cosmo, term, th6, lmax, theta_max, tmy, x, n, out);
 }
 
 extern "C" int tp_ctx_set_cov_tolerance(tp_ctx* ctx, int term, double rel_tol) {

@@ -20,8 +20,9 @@ double halo_lmax(int term, const double* t);
 int ensure_halo(tp_ctx* ctx, int cosmo);
 
 // The halo integral of T5, T6 or T7 for each radius set th6[i] (T6 without
-// its 1-D ell_1 factor), normalised as the reference normalises them.
+// its 1-D ell_1 factor), normalised as the reference normalises them;
+// precision TP_FP64 or TP_FP32 (node arithmetic; the cubature is FP64).
 int halo_terms(tp_ctx* ctx, int cosmo, int term, int geom, double theta_max, double area,
-               const std::vector<std::array<double, 6>>& th6, std::vector<double>& out, int& bad);
+               const std::vector<std::array<double, 6>>& th6, int precision, std::vector<double>& out, int& bad);
 
 }  // namespace tp

@@ -151,9 +151,13 @@ enum HaloNodeRow {
 
 // Halo-model tables of one cosmology: sigma^2(m_i) and dsigma^2/dm(m_i) at
 // z = 0 for m_i = 10^(LOGM_MIN + i (LOGM_MAX - LOGM_MIN) / NM), and the node rows.
+// hnf holds the same rows in FP32 with the two weight rows divided by their
+// largest node value, wmax[0] (HN_WTRI) and wmax[1] (HN_WPEN).
 struct HaloTab {
   double sig2[NM], dsig2[NM];
   double hn[HN_COUNT * NNODE];
+  float hnf[HN_COUNT * NNODE];
+  double wmax[2];
 };
 
 // ---- helpers shared by several translation units ---------------------------
