@@ -597,6 +597,89 @@ def run_cov(args):
             "fp64": {"pairs": n64, "seconds_per_term": t64, "rel_err_fp32_vs_fp64": err}}
 
 
+def run_halo(args):
+    """Halo-model covariance terms (T5, T7 infinite survey with the 100 deg^2
+    area; T6 the square 10x10 deg^2 window) for a seeded sample of the 24310
+    triplet pairs of the 220 triplets; sigma_eps 0.3, n_gal 10 arcmin^-2. The
+    FP32 node path is timed through the host API; FP64 reruns a few pairs for
+    the per-output difference; the CPU oracle integrates the first distinct
+    integral of each term on the host cores (a bounded sample: 5-30 s)."""
+    import torch
+
+    import threepoint_gb300 as tp
+
+    rank, world, local = dist_env()
+    if rank != 0:
+        return None
+    torch.cuda.set_device(local)
+    ctx = tp.Context(local)
+    zs, ns = nz_config()
+    nz = tp.rebin_n_of_z(zs, ns, 256, 3.0)
+    sig, ngal = 0.3, 10 / ARCMIN ** 2
+    ctx.set_shape_noise(sig, ngal, False)
+    ctx.set_cosmology(tp.cosmology(**COSMO_FID), nz)
+    th = thetas_220()
+    pairs = [(i, j) for i in range(len(th)) for j in range(i, len(th))]
+    rng = np.random.default_rng(LHS_SEED)
+    pick = rng.choice(len(pairs), size=min(args.halo_pairs, len(pairs)), replace=False)
+    A = np.array([th[pairs[k][0]] for k in pick])
+    B = np.array([th[pairs[k][1]] for k in pick])
+    deg = 0.017453
+    kw = dict(thetaMax=10 * deg, area=100 * deg * deg)
+    all_terms = {"T5": (5, tp.GEOM_INFINITE), "T6": (6, tp.GEOM_SQUARE), "T7": (7, tp.GEOM_INFINITE)}
+    terms = tuple((n, *all_terms[n]) for n in args.halo_terms.split(","))
+    ctx.halo_tables()  # table build outside the timed region
+    res, t, capped = {}, {}, {}
+    for name, term, geom in terms:
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        res[name] = ctx.cov_total(term, A, B, geometry=geom, precision=tp.FP32, check=False, **kw)
+        t[name] = time.perf_counter() - t0
+        capped[name] = ctx.last_capped
+    n64 = min(len(pick), args.halo_fp64_pairs)
+    err, t64 = {}, {}
+    for name, term, geom in terms:
+        if n64 == 0 or name not in args.halo_fp64_terms.split(","):
+            continue
+        t0 = time.perf_counter()
+        r64 = ctx.cov_total(term, A[:n64], B[:n64], geometry=geom, precision=tp.FP64, check=False, **kw)
+        t64[name] = time.perf_counter() - t0
+        err[name] = _rel_stats(res[name][:n64], r64)
+    ctx.close()
+    tot = sum(t.values())
+    cpu = None
+    if not args.no_cpu_baseline and args.halo_cpu_terms:
+        import oracle as O
+
+        O.set_threads(0)
+        T = O.Tables(COSMO_FID, nz)
+        T.set_noise(sig, ngal, False)
+        cpu_s, cpu_terms = 0.0, []
+        for name in args.halo_cpu_terms.split(","):
+            term, geom = all_terms[name]
+            mult_idx = O.halo_total_terms(term, A[0], B[0])
+            src = list(A[0]) + list(B[0])
+            th6 = [src[i] for i in mult_idx[0][1]]
+            par = O.CovParams(geom, kw["thetaMax"], kw["area"], 0.0)
+            t0 = time.perf_counter()
+            T.cov_T_halo(term, par, th6)
+            cpu_s += time.perf_counter() - t0
+            cpu_terms.append(name)
+        cpu = {"value": len(cpu_terms) / cpu_s, "unit": "integrals/s", "cores": os.cpu_count(), "kind": "port",
+               "sample": f"the first integral of the first pair for {','.join(cpu_terms)} at the reference's "
+                         f"tolerances (FP64 oracle, {os.cpu_count()} threads)"}
+    return {"metric": f"<Map^3> covariance halo-model entries/s ({args.halo_terms}; T5, T7 infinite with the "
+                      f"100 deg^2 area, T6 square 10x10 deg^2)",
+            "value": len(pick) / tot, "unit": "entries/s", "n_gpus": 1, "steps": 1, "warmup": 0,
+            "ms_per_step": tot * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic",
+            "config": {"workload": f"{len(pick)} of the 24310 triplet pairs of 220 triplets (seeded sample)",
+                       "seconds_per_term": t, "timing": "host API tp_cov_total_batch",
+                       "integrals_at_region_cap": capped},
+            "fp64": {"pairs": n64, "seconds_per_term": t64, "rel_err_fp32_vs_fp64": err},
+            "cpu_baseline": cpu}
+
+
 def run_plain(args):
     """The plain form (FP64 BiHalofit, FP64 cubature) on the fiducial
     cosmology and the 20 triplets of radii {2, 4, 8, 16}', through the host
@@ -897,20 +980,27 @@ def main():
     ap.add_argument("--no-fp64-plain", action="store_true", help="skip the plain FP64 comparison run")
     ap.add_argument("--no-pipeline", action="store_true", help="one context, steps run one after another")
     ap.add_argument("--apm-npix", type=int, default=4096, help="pixels per side of the aperture-mass grid")
-    ap.add_argument("--workload", default="map3", choices=["map3", "gamma", "cov", "surrogate", "plain", "apm"],
-                    help="map3: the headline metric; gamma / cov: the shear-3PCF grid and covariance "
-                         "configurations; surrogate: training and accuracy of the b_kappa network; plain: the "
-                         "FP64 form on the fiducial 20 triplets; apm: the FFT aperture-mass measurement")
+    ap.add_argument("--workload", default="map3",
+                    choices=["map3", "gamma", "cov", "halo", "surrogate", "plain", "apm"],
+                    help="map3: the headline metric; gamma / cov / halo: the shear-3PCF grid and covariance "
+                         "configurations (halo: the halo-model terms T5-T7); surrogate: training and accuracy of "
+                         "the b_kappa network; plain: the FP64 form on the fiducial 20 triplets; apm: the FFT "
+                         "aperture-mass measurement")
     ap.add_argument("--gamma-triangles", type=int, default=0, help="first N triangles of the grid (0 = all 1000)")
     ap.add_argument("--gamma-fp64-sample", type=int, default=20)
     ap.add_argument("--gamma-region-cap", type=int, default=32768,
                     help="regions per Gamma integral (the grid's small triangles need more than the default)")
     ap.add_argument("--cov-pairs", type=int, default=24)
     ap.add_argument("--cov-fp64-pairs", type=int, default=4)
-    ap.add_argument("--cov-terms", default="T1,T2,T4", help="comma-separated subset of T1,T2,T4")
+    ap.add_argument("--cov-terms", default="T1,T2,T4", help="comma-separated subset of T1,T2,T4 (T5-T7: --workload halo)")
     ap.add_argument("--cov-fp64-terms", default="T2,T4",
                     help="terms also run in FP64 for the error (the square T1 at the cap takes minutes in FP64)")
     ap.add_argument("--cov-region-cap", type=int, default=0, help="regions per covariance integral (0: library default)")
+    ap.add_argument("--halo-pairs", type=int, default=32)
+    ap.add_argument("--halo-terms", default="T5,T7", help="comma-separated subset of T5,T6,T7")
+    ap.add_argument("--halo-fp64-pairs", type=int, default=2)
+    ap.add_argument("--halo-fp64-terms", default="T7", help="terms also run in FP64 (one FP64 T5 integral ~1 min)")
+    ap.add_argument("--halo-cpu-terms", default="T7", help="terms the CPU oracle samples (one integral each)")
     ap.add_argument("--sg-cosmo", type=int, default=64)
     ap.add_argument("--sg-points", type=int, default=1 << 18, help="training triangles per cosmology")
     ap.add_argument("--sg-holdout", type=int, default=8)
@@ -926,6 +1016,8 @@ def main():
         res = run_gamma(args)
     elif args.workload == "cov":
         res = run_cov(args)
+    elif args.workload == "halo":
+        res = run_halo(args)
     elif args.workload == "surrogate":
         res = run_surrogate(args)
     elif args.workload == "plain":

@@ -355,6 +355,11 @@ int tp_cov_term_batch(tp_ctx* ctx, int cosmo_index, int term, int geometry, doub
  * 1271, 1307). */
 int tp_ctx_set_cov_tolerance(tp_ctx* ctx, int term, double rel_tol);
 
+/* CTAs that integrate one T5/T6/T7 integral together: 8 (default; a
+ * thread-block cluster of 8 CTAs deals out each sweep's regions) or 1 (one
+ * CTA per integral). The results are the same bit for bit. */
+int tp_ctx_set_halo_cluster(tp_ctx* ctx, int ctas);
+
 /* Halo model of T5-T7 (cuda_version/halomodel.cu), built per cosmology on
  * first use.
  * tp_halo_tables: out[0..127] = sigma^2(m_i), out[128..255] = dsigma^2/dm(m_i)

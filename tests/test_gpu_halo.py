@@ -193,3 +193,23 @@ def test_geometry_rules(halo_ctx):
         halo_ctx.cov_total(6, [TH6[:3]], [TH6[3:]], geometry=0, thetaMax=TMAX, area=AREA)
     # T6_total is 0 for the infinite survey
     assert halo_ctx.cov_total(6, [TH6[:3]], [TH6[3:]], geometry=2, thetaMax=TMAX, area=AREA)[0] == 0.0
+
+
+@pytest.mark.parametrize("prec", [0, 1])
+def test_cluster_of_eight_equals_one_cta(halo_ctx, prec):
+    """Eight CTAs of a thread-block cluster sharing each integral refine the
+    same regions as one CTA: identical values, for a batch of distinct
+    integrals (the job loop of the clusters) in both precisions."""
+    ths = [TH6, [4 * ARC, 8 * ARC, 8 * ARC, 8 * ARC, 8 * ARC, 16 * ARC],
+           [16 * ARC, 16 * ARC, 16 * ARC, 8 * ARC, 16 * ARC, 32 * ARC]]
+    halo_ctx.set_cov_tolerance(5, LOOSE[5])
+    try:
+        halo_ctx.set_halo_cluster(1)
+        one = halo_ctx.cov_term(5, ths, geometry=2, thetaMax=TMAX, area=AREA, precision=prec)
+        halo_ctx.set_halo_cluster(8)
+        eight = halo_ctx.cov_term(5, ths, geometry=2, thetaMax=TMAX, area=AREA, precision=prec)
+    finally:
+        halo_ctx.set_halo_cluster(8)
+        halo_ctx.set_cov_tolerance(5, 0.0)
+    assert np.array_equal(one, eight)
+    assert np.all(np.isfinite(one)) and np.all(one != 0)

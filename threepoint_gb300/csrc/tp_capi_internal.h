@@ -53,6 +53,8 @@ struct tp_ctx {
   // halo-model tables (covariance terms T5-T7), built per cosmology on first use
   tp::HaloTab* d_halo = nullptr;
   std::vector<char> halo_ready;
+  // CTAs that share one T5-T7 integral (a thread-block cluster; 1 or 8)
+  int halo_cluster = 8;
   // relative tolerance of the T5, T6, T7 integrals (index 5..7); 0 = the reference's
   double cov_rel_tol[8] = {0, 0, 0, 0, 0, 0, 0, 0};
 

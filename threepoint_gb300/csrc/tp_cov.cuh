@@ -88,44 +88,67 @@ struct JobSet {
   }
 };
 
-// Runs the adaptive engine over njobs integrals of policy P (one CTA per
-// integral, persistent grid), each to relative tolerance rel_tol in the L1 norm.
-template <int DIM, class P, int NT>
+// Runs the adaptive engine over njobs integrals of policy P, each to relative
+// tolerance rel_tol in the L1 norm, on a persistent grid: one CTA per
+// integral (CS = 1) or one cluster of CS CTAs per integral (CS > 1, the
+// cooperative form of adaptive_body, for integrands whose points are costly
+// enough that one integral should spread over several SMs).
+template <int DIM, class P, int NT, int CS>
 __global__ void __launch_bounds__(NT) k_cov(P pol_in, int njobs, int* job_counter, EngineCfg cfg, char* scratch,
                                             size_t slot_bytes) {
   P pol = pol_in;
   pol.loaded = 0;
-  adaptive_body<DIM, 1, NT, P>(pol, njobs, job_counter, cfg, scratch, slot_bytes);
+  adaptive_body<DIM, 1, NT, P, CS>(pol, njobs, job_counter, cfg, scratch, slot_bytes);
 }
 
-template <int DIM, class P>
+template <int DIM, class P, int CS = 1>
 inline int run_engine(tp_ctx* ctx, const P& pol, int njobs, double rel_tol) {
   constexpr int NT = 256;
   if (njobs == 0) return TP_OK;
+  auto kern = k_cov<DIM, P, NT, CS>;
   size_t smem = engine_smem_bytes<DIM, 1, P>();
-  cudaError_t e = cudaFuncSetAttribute(k_cov<DIM, P, NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return tp_cuda(ctx, e, "cov attribute");
-  int sms = 0, per_sm = 0;
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
-  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cov<DIM, P, NT>, NT, smem);
-  if (e != cudaSuccess || per_sm < 1) return tp_cuda(ctx, e ? e : cudaErrorInvalidConfiguration, "cov occupancy");
-  int grid = sms * per_sm;
-  if (ctx->max_ctas > 0 && grid > ctx->max_ctas) grid = ctx->max_ctas;
-  if (grid > njobs) grid = njobs;
+  cudaLaunchConfig_t lc = {};
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = CS;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  lc.blockDim = dim3(NT);
+  lc.dynamicSmemBytes = smem;
+  lc.stream = ctx->stream;
+  lc.attrs = attr;
+  lc.numAttrs = CS > 1 ? 1 : 0;
+  int units = 0;  // integrals in flight: CTAs (CS = 1) or clusters
+  if constexpr (CS == 1) {
+    int sms = 0, per_sm = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, NT, smem);
+    if (e != cudaSuccess || per_sm < 1) return tp_cuda(ctx, e ? e : cudaErrorInvalidConfiguration, "cov occupancy");
+    units = sms * per_sm;
+  } else {
+    lc.gridDim = dim3(CS);
+    e = cudaOccupancyMaxActiveClusters(&units, (const void*)kern, &lc);
+    if (e != cudaSuccess || units < 1)
+      return tp_cuda(ctx, e ? e : cudaErrorInvalidConfiguration, "cov cluster occupancy");
+  }
+  if (ctx->max_ctas > 0 && units * CS > ctx->max_ctas) units = std::max(1, ctx->max_ctas / CS);
+  if (units > njobs) units = njobs;
   // covariance integrals (6-D square-window T1, oscillating 2-D T2) refine to
   // 10^5 regions and more: at least 2^19 regions per integral, with the grid
   // trimmed so that the region stores stay within 64 GB of HBM
   const int cap = std::max(ctx->region_cap, 1 << 19);
   size_t slot = Slot<DIM, 1>::bytes(cap);
   const size_t budget = size_t(64) << 30;
-  if ((size_t)grid * slot > budget) grid = std::max(1, (int)(budget / slot));
-  int st = ctx->ensure_scratch((size_t)grid * slot);
+  if ((size_t)units * slot > budget) units = std::max(1, (int)(budget / slot));
+  int st = ctx->ensure_scratch((size_t)units * slot);
   if (st) return st;
   EngineCfg cfg{0.0, rel_tol, TP_NORM_L1, cap, 4000};
   e = cudaMemsetAsync(ctx->d_counter, 0, sizeof(int), ctx->stream);
   if (e == cudaSuccess) {
-    k_cov<DIM, P, NT><<<grid, NT, smem, ctx->stream>>>(pol, njobs, ctx->d_counter, cfg, ctx->d_scratch, slot);
-    e = cudaGetLastError();
+    lc.gridDim = dim3(units * CS);
+    e = cudaLaunchKernelEx(&lc, kern, pol, njobs, ctx->d_counter, cfg, ctx->d_scratch, slot);
   }
   if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
   return tp_cuda(ctx, e, "cov launch");

@@ -20,6 +20,7 @@
 // (8 passes of 256-bin shared-memory histograms) followed by a block-wide
 // stream compaction; no sort and no host round trip.
 #pragma once
+#include <cooperative_groups.h>
 #include <stdint.h>
 
 #include "tp_internal.cuh"
@@ -339,7 +340,28 @@ __host__ __device__ constexpr size_t engine_smem_bytes() {
 //   __device__ void finalize(const char* rec, const double* sum /*FDIM*/, double* fval /*FDIM*/)
 //   __device__ void end_job(int job, const double* V, const double* E, long long neval, int status)
 //   static constexpr size_t PSMEM (policy shared bytes)
-template <int DIM, int FDIM, int NT, class P>
+//
+// CS > 1 (launch with thread-block clusters of CS CTAs): the CTAs of a
+// cluster own one integral together. Every sweep's pending regions are dealt
+// out to them in chunks (rank r takes chunks r, r + CS, ...); the region store
+// is the cluster's, in HBM; rank 0 alone does the totals, the selection and
+// the splitting, and publishes the job, the pending count and the stop flag
+// in its shared memory, which the other ranks read through distributed shared
+// memory. Two cluster barriers per sweep (after the evaluation, after the
+// bookkeeping), with release/acquire ordering of the region store; every rank
+// takes the same branches, decided from rank 0's published values after a
+// barrier. The region sequence is that of CS = 1.
+template <int CS>
+__device__ __forceinline__ void engine_cluster_sync() {
+  if constexpr (CS > 1) {
+    __threadfence();
+    cooperative_groups::this_cluster().sync();
+  } else {
+    __syncthreads();
+  }
+}
+
+template <int DIM, int FDIM, int NT, class P, int CS = 1>
 __device__ void adaptive_body(P& pol, int njobs, int* job_counter, const EngineCfg cfg, char* scratch,
                               size_t slot_bytes) {
   constexpr int NP = GMRule<DIM>::NP;
@@ -354,23 +376,32 @@ __device__ void adaptive_body(P& pol, int njobs, int* job_counter, const EngineC
   double* part = (double*)(recs + (((size_t)CH * NP * P::REC + 15) & ~size_t(15)));  // [G][CH*NP][PD]
   double* fval = part + (size_t)G * CH * NP * PD;                                 // [CH*NP][FDIM]
   EngineShared<FDIM>* es = (EngineShared<FDIM>*)(fval + (size_t)CH * NP * FDIM);
+  // the control block every rank follows: rank 0's (distributed shared memory)
+  EngineShared<FDIM>* es0 = es;
+  int crank = 0;
+  if constexpr (CS > 1) {
+    cooperative_groups::cluster_group cl = cooperative_groups::this_cluster();
+    crank = (int)cl.block_rank();
+    es0 = cl.map_shared_rank(es, 0);
+  }
 
   Slot<DIM, FDIM> S;
-  S.init(scratch + (size_t)blockIdx.x * slot_bytes, cfg.cap);
+  S.init(scratch + (size_t)(blockIdx.x / CS) * slot_bytes, cfg.cap);
   const int tid = threadIdx.x;
 
   for (;;) {
-    if (tid == 0) {
+    if (crank == 0 && tid == 0) {
       int k = atomicAdd(job_counter, 1);
       es->job = (k < njobs && pol.job_order) ? pol.job_order[k] : k;
       es->ktot = k;
     }
-    __syncthreads();
-    const int job = es->job;
-    if (es->ktot >= njobs) break;
+    engine_cluster_sync<CS>();
+    const int job = es0->job;
+    if (es0->ktot >= njobs) break;
     double xmin[DIM], xmax[DIM];
     pol.begin_job(job, psmem, xmin, xmax);
-    if (tid == 0) {
+    if (tid == 0) es->nlive_chunk = 0;
+    if (crank == 0 && tid == 0) {
       for (int d = 0; d < DIM; ++d) {
         S.cen[(size_t)d * S.cap] = 0.5 * (xmin[d] + xmax[d]);
         S.hw[(size_t)d * S.cap] = 0.5 * (xmax[d] - xmin[d]);
@@ -385,14 +416,13 @@ __device__ void adaptive_body(P& pol, int njobs, int* job_counter, const EngineC
       es->stop = 0;
       es->neval = 0;
       es->sweeps = 0;
-      es->nlive_chunk = 0;
     }
-    __syncthreads();
+    engine_cluster_sync<CS>();
 
     for (int sweep = 0;; ++sweep) {
       // ---------------- evaluate the pending regions ----------------------
-      const int npend = es->npend;
-      for (int base = 0; base < npend; base += CH) {
+      const int npend = es0->npend;
+      for (int base = crank * CH; base < npend; base += CS * CH) {
         const int nreg = min(CH, npend - base);
         const int npts = nreg * NP;
         // (a) point setup; points that need the expensive inner sums are
@@ -452,6 +482,10 @@ __device__ void adaptive_body(P& pol, int njobs, int* job_counter, const EngineC
         }
         __syncthreads();
       }
+      if constexpr (CS > 1) engine_cluster_sync<CS>();
+      // rank 0: totals, convergence, selection and splitting; a stop sets
+      // es->stop and leaves this block
+      if (crank == 0) do {
       if (tid == 0) es->neval += (long long)npend * NP;
 
       // ---------------- totals and convergence ----------------------------
@@ -476,6 +510,7 @@ __device__ void adaptive_body(P& pol, int njobs, int* job_counter, const EngineC
           }
           if (!conv) es->status |= 2;
           es->sweeps = sweep + 1;
+          es->stop = 1;
         }
         __syncthreads();
         break;
@@ -590,6 +625,7 @@ __device__ void adaptive_body(P& pol, int njobs, int* job_counter, const EngineC
           }
           es->status |= (ktot == 0) ? 4 : 1;
           es->sweeps = sweep + 1;
+          es->stop = 1;
         }
         __syncthreads();
         break;
@@ -625,11 +661,15 @@ __device__ void adaptive_body(P& pol, int njobs, int* job_counter, const EngineC
         es->nlive = nlive + ktot;
         es->npend = 2 * ktot;
       }
-      __syncthreads();
+      } while (0);
+      engine_cluster_sync<CS>();
+      if (es0->stop) break;
     }
-    pol.end_job(job, es->V, es->E, es->neval, es->status);
+    if (crank == 0) pol.end_job(job, es->V, es->E, es->neval, es->status);
     __syncthreads();
   }
+  // no rank leaves while another may still read rank 0's shared memory
+  if constexpr (CS > 1) cooperative_groups::this_cluster().sync();
 }
 
 

@@ -605,7 +605,13 @@ int run_halo_kind(tp_ctx* ctx, int cosmo, const JobSet& js, double theta_max, do
   pol.jobs = (const CovJob*)(b + o_j);
   pol.out = (double*)(b + o_o);
   pol.status = (int*)(b + o_s);
-  st = run_engine<HaloProd<KIND, R>::DIM>(ctx, pol, (int)n, rel_tol);
+  // one cluster of 8 CTAs per integral: a T5-T7 point costs 96 nodes x 4-6
+  // NFW profiles, so a single integral (or the most expensive one of a batch)
+  // spreads over 8 SMs; the region sequence is that of one CTA per integral
+  if (ctx->halo_cluster > 1)
+    st = run_engine<HaloProd<KIND, R>::DIM, HaloProd<KIND, R>, 8>(ctx, pol, (int)n, rel_tol);
+  else
+    st = run_engine<HaloProd<KIND, R>::DIM, HaloProd<KIND, R>, 1>(ctx, pol, (int)n, rel_tol);
   if (st) return st;
   std::vector<int> hs(n);
   e = cudaMemcpy(res.data(), b + o_o, sizeof(double) * n, cudaMemcpyDeviceToHost);
@@ -775,6 +781,12 @@ extern "C" int tp_halo_integrand_points(tp_ctx* ctx, int cosmo, int term, int ge
   const double tmy = geometry == TP_GEOM_RECTANGLE ? ctx->theta_max_smaller : theta_max;
   return precision == TP_FP32 ? halo_points_t<float>(ctx, cosmo, term, th6, lmax, theta_max, tmy, x, n, out)
                               : halo_points_t<double>(ctx, cosmo, term, th6, lmax, theta_max, tmy, x, n, out);
+}
+
+extern "C" int tp_ctx_set_halo_cluster(tp_ctx* ctx, int ctas) {
+  if (!ctx || (ctas != 1 && ctas != 8)) return TP_ERR_ARG;
+  ctx->halo_cluster = ctas;
+  return TP_OK;
 }
 
 extern "C" int tp_ctx_set_cov_tolerance(tp_ctx* ctx, int term, double rel_tol) {
