@@ -11,7 +11,9 @@
 //   gamma0..gamma3, compute_weights_bessel (gamma.cuh:56-97,291),
 //   the covariance globals type, thetaMax, thetaMax_smaller, area, lMin,
 //   sigma, n, constant_powerspectrum and initCovariance, T1_total, T2_total,
-//   T4_total (apertureStatisticsCovariance.cuh:22-54,116-136; bispectrum.cuh:19,29).
+//   T4_total, T5_total, T6_total, T7_total, initHalomodel
+//   (apertureStatisticsCovariance.cuh:22-54,116-136; bispectrum.cuh:19,29;
+//   halomodel.cuh).
 // Differences: errors throw std::runtime_error (or std::invalid_argument)
 // where the reference prints and calls exit(); all evaluations are FP64 (the
 // reference's arithmetic); gamma*'s z_max must be the cosmology's zmax (the
@@ -193,4 +195,16 @@ inline double T2_total(const std::vector<double>& thetas_123, const std::vector<
 }
 inline double T4_total(const std::vector<double>& thetas_123, const std::vector<double>& thetas_456) {
   return threepoint_gb300_detail::cov_total(4, thetas_123, thetas_456);
+}
+// halo-model terms (apertureStatisticsCovariance.cu:685-1044); the halo model
+// (initHalomodel, halomodel.cu:18-29) is built on first use
+inline void initHalomodel() {}
+inline double T5_total(const std::vector<double>& thetas_123, const std::vector<double>& thetas_456) {
+  return threepoint_gb300_detail::cov_total(5, thetas_123, thetas_456);
+}
+inline double T6_total(const std::vector<double>& thetas_123, const std::vector<double>& thetas_456) {
+  return threepoint_gb300_detail::cov_total(6, thetas_123, thetas_456);
+}
+inline double T7_total(const std::vector<double>& thetas_123, const std::vector<double>& thetas_456) {
+  return threepoint_gb300_detail::cov_total(7, thetas_123, thetas_456);
 }

@@ -101,8 +101,8 @@ __global__ void __launch_bounds__(NT) k_cov(P pol_in, int njobs, int* job_counte
   adaptive_body<DIM, 1, NT, P, CS>(pol, njobs, job_counter, cfg, scratch, slot_bytes);
 }
 
-template <int DIM, class P, int CS = 1>
-inline int run_engine(tp_ctx* ctx, const P& pol, int njobs, double rel_tol) {
+template <int DIM, class P, int CS>
+inline int run_engine_cs(tp_ctx* ctx, const P& pol, int njobs, double rel_tol) {
   constexpr int NT = 256;
   if (njobs == 0) return TP_OK;
   auto kern = k_cov<DIM, P, NT, CS>;
@@ -152,6 +152,32 @@ inline int run_engine(tp_ctx* ctx, const P& pol, int njobs, double rel_tol) {
   }
   if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
   return tp_cuda(ctx, e, "cov launch");
+}
+
+// cluster: 1 = one CTA per integral, 8 = one 8-CTA cluster per integral,
+// 0 = 8 when the batch has no more integrals than the device has CTA slots
+// (a smaller batch would leave SMs idle, and its most expensive integral
+// would set the time), else 1. A policy whose clusters do not fit runs with 1.
+template <int DIM, class P>
+inline int run_engine(tp_ctx* ctx, const P& pol, int njobs, double rel_tol, int cluster = 0) {
+  constexpr int NT = 256;
+  if (njobs == 0) return TP_OK;
+  if (cluster == 0) {
+    int sms = 0, per_sm = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
+    size_t smem = engine_smem_bytes<DIM, 1, P>();
+    cudaFuncSetAttribute(k_cov<DIM, P, NT, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cov<DIM, P, NT, 1>, NT, smem) != cudaSuccess)
+      per_sm = 1;
+    cudaGetLastError();
+    cluster = njobs <= sms * per_sm ? 8 : 1;
+  }
+  if (cluster == 8) {
+    const int st = run_engine_cs<DIM, P, 8>(ctx, pol, njobs, rel_tol);
+    if (st != TP_ERR_CUDA || ctx->err.find("cluster occupancy") == std::string::npos) return st;
+    cudaGetLastError();  // no 8-CTA cluster of this policy fits: one CTA per integral
+  }
+  return run_engine_cs<DIM, P, 1>(ctx, pol, njobs, rel_tol);
 }
 
 }  // namespace tp

@@ -544,7 +544,7 @@ int ensure_halo(tp_ctx* ctx, int cosmo) {
   pol.rhobar = RHO_CRIT * ctx->h_cos[cosmo].om;
   pol.out = (double*)b;
   pol.status = (int*)(b + o_s);
-  st = run_engine<1>(ctx, pol, 2 * NM, 1e-4);
+  st = run_engine<1>(ctx, pol, 2 * NM, 1e-4, 1);
   if (st) return st;
   std::vector<int> hs(2 * NM);
   e = cudaMemcpy(hs.data(), b + o_s, sizeof(int) * 2 * NM, cudaMemcpyDeviceToHost);
@@ -608,10 +608,7 @@ int run_halo_kind(tp_ctx* ctx, int cosmo, const JobSet& js, double theta_max, do
   // one cluster of 8 CTAs per integral: a T5-T7 point costs 96 nodes x 4-6
   // NFW profiles, so a single integral (or the most expensive one of a batch)
   // spreads over 8 SMs; the region sequence is that of one CTA per integral
-  if (ctx->halo_cluster > 1)
-    st = run_engine<HaloProd<KIND, R>::DIM, HaloProd<KIND, R>, 8>(ctx, pol, (int)n, rel_tol);
-  else
-    st = run_engine<HaloProd<KIND, R>::DIM, HaloProd<KIND, R>, 1>(ctx, pol, (int)n, rel_tol);
+  st = run_engine<HaloProd<KIND, R>::DIM>(ctx, pol, (int)n, rel_tol, ctx->halo_cluster);
   if (st) return st;
   std::vector<int> hs(n);
   e = cudaMemcpy(res.data(), b + o_o, sizeof(double) * n, cudaMemcpyDeviceToHost);
