@@ -360,6 +360,11 @@ int tp_ctx_set_cov_tolerance(tp_ctx* ctx, int term, double rel_tol);
  * CTA per integral). The results are the same bit for bit. */
 int tp_ctx_set_halo_cluster(tp_ctx* ctx, int ctas);
 
+/* <Map^3> calls (tp_map3_batch, tp_map3_jobs_device) with no more integrals
+ * than the device has CTA slots run one 8-CTA cluster per integral when on
+ * (1, default); 0 keeps one CTA per integral. Same results bit for bit. */
+int tp_ctx_set_map3_cluster(tp_ctx* ctx, int on);
+
 /* Halo model of T5-T7 (cuda_version/halomodel.cu), built per cosmology on
  * first use.
  * tp_halo_tables: out[0..127] = sigma^2(m_i), out[128..255] = dsigma^2/dm(m_i)

@@ -271,3 +271,22 @@ def test_map3_fp64_matches_oracle_at_box_corner(nz256):
             continue
         assert got[0, t] == pytest.approx(ref, rel=1e-6), (np.array(th) / ARC, got[0, t], ref)
         assert abs(int(info["neval"][0, t]) - nev) <= 0.01 * nev
+
+
+@pytest.mark.parametrize("prec", [0, 1])
+def test_map3_cluster_equals_one_cta(gpu_ctx, prec):
+    """A batch smaller than the device's CTA slots runs one 8-CTA cluster per
+    integral; the same regions are refined as with one CTA, so values, error
+    estimates and evaluation counts are identical."""
+    r = np.array([2.0, 4.0, 8.0, 16.0]) * ARC
+    th = np.array([(r[i], r[j], r[k]) for i in range(4) for j in range(i, 4) for k in range(j, 4)])
+    try:
+        gpu_ctx.set_map3_cluster(False)
+        a, ia = gpu_ctx.map3_batch(th, cosmo_index=[0], precision=prec, return_info=True)
+        gpu_ctx.set_map3_cluster(True)
+        b, ib = gpu_ctx.map3_batch(th, cosmo_index=[0], precision=prec, return_info=True)
+    finally:
+        gpu_ctx.set_map3_cluster(True)
+    assert np.array_equal(a, b)
+    assert np.array_equal(ia["err"], ib["err"]) and np.array_equal(ia["neval"], ib["neval"])
+    assert np.all(np.isfinite(a))

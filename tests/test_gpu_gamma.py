@@ -97,3 +97,19 @@ def test_gamma_region_cap_escalation_matches_oracle(nz256, oracle_tables):
         assert ctx.last_gamma_status[0] == 0
     assert got == once
     assert abs(got - ref) <= 1e-4 * abs(ref), (got, ref)
+
+
+def test_gamma_small_batch_clusters_equal_large_batch(gpu_ctx):
+    """A batch with no more integrals than CTA slots runs one 8-CTA cluster per
+    integral, a large batch one CTA per integral; both refine the same regions,
+    so a triangle's four components are identical either way."""
+    rng = np.random.default_rng(4)
+    n = 320
+    r1 = rng.uniform(4, 12, n) * ARC
+    r2 = r1 * rng.uniform(0.7, 1.0, n)
+    r3 = np.abs(r1 - r2) + (r1 + r2 - np.abs(r1 - r2)) * rng.uniform(0.3, 0.7, n)
+    tri = np.column_stack([r1, r2, r3])
+    big = gpu_ctx.gamma_batch(tri, precision=1)     # 1280 integrals: one CTA each
+    small = gpu_ctx.gamma_batch(tri[:3], precision=1)  # 12 integrals: 8-CTA clusters
+    assert np.array_equal(big[:3], small)
+    assert np.all(np.isfinite(big))

@@ -187,6 +187,7 @@ def lib():
         L.tp_halo_integrand_points.argtypes = [p, i, i, i, d, dp, dp, l, i, dp]
         L.tp_ctx_set_cov_tolerance.argtypes = [p, i, d]
         L.tp_ctx_set_halo_cluster.argtypes = [p, i]
+        L.tp_ctx_set_map3_cluster.argtypes = [p, i]
         L.tp_cov_params_from_file.argtypes = [C.c_char_p, C.POINTER(_CovParams)]
         L.tp_gamma_config_from_file.argtypes = [C.c_char_p, C.POINTER(_GammaConfig)]
         L.tp_gamma_triangles.argtypes = [C.POINTER(_GammaConfig), dp, dp]
@@ -522,6 +523,11 @@ class Context:
         """Relative tolerance of the T5/T6/T7 integrals (0 = the reference's
         1e-2 / 1e-1 / 1e-1)."""
         _check(self._h, lib().tp_ctx_set_cov_tolerance(self._h, term, rel_tol))
+
+    def set_map3_cluster(self, on=True):
+        """<Map^3> batches with no more integrals than CTA slots: one 8-CTA
+        cluster per integral (on) or one CTA (off)."""
+        _check(self._h, lib().tp_ctx_set_map3_cluster(self._h, int(bool(on))))
 
     def set_halo_cluster(self, ctas=8):
         """CTAs per T5/T6/T7 integral: 8 (a thread-block cluster) or 1."""

@@ -597,9 +597,10 @@ extern "C" int tp_map3_jobs_device(tp_ctx* ctx, const int* job_cosmo, const doub
   if (ctx->n_cosmo == 0) return tp_fail(ctx, TP_ERR_STATE, "no cosmology set");
   if (n_jobs == 0) return TP_OK;
   cudaSetDevice(ctx->device);
-  int grid = 0;
+  int grid = 0, cluster = 1;
   size_t smem = 0, scratch = 0;
-  cudaError_t e = plan_map3(precision, n_jobs, ctx->region_cap, ctx->max_ctas, &grid, &smem, &scratch);
+  cudaError_t e = plan_map3(precision, n_jobs, ctx->region_cap, ctx->max_ctas, ctx->map3_cluster, &grid, &cluster,
+                            &smem, &scratch);
   if (e != cudaSuccess) return tp_cuda(ctx, e, "map3 plan");
   int st = ctx->ensure_scratch(scratch);
   if (st) return st;
@@ -630,6 +631,7 @@ extern "C" int tp_map3_jobs_device(tp_ctx* ctx, const int* job_cosmo, const doub
   L.job_counter = ctx->d_counter;
   L.diag = ctx->d_diag;
   L.job_order = job_order;
+  L.cluster = cluster;
   e = launch_map3(L, grid, smem, ctx->d_scratch, ctx->stream);
   return tp_cuda(ctx, e, "map3 launch");
 }

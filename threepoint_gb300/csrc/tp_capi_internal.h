@@ -55,6 +55,9 @@ struct tp_ctx {
   std::vector<char> halo_ready;
   // CTAs that share one T5-T7 integral (a thread-block cluster; 1 or 8)
   int halo_cluster = 8;
+  // <Map^3> host calls with no more integrals than CTA slots run one 8-CTA
+  // cluster per integral (0: always one CTA per integral)
+  int map3_cluster = 1;
   // relative tolerance of the T5, T6, T7 integrals (index 5..7); 0 = the reference's
   double cov_rel_tol[8] = {0, 0, 0, 0, 0, 0, 0, 0};
 

@@ -512,22 +512,13 @@ static int run_pell_kind(tp_ctx* ctx, int cosmo, const JobSet& js, double theta_
                          double norm, double rel_tol, std::vector<double>& res, int& bad) {
   res.assign(js.jobs.size(), 0.0);
   if (js.jobs.empty()) return TP_OK;
-  const size_t n = js.jobs.size();
-  size_t o_j = 0, o_o = (sizeof(CovJob) * n + 255) & ~size_t(255);
-  size_t o_s = o_o + ((sizeof(double) * n + 255) & ~size_t(255));
-  int st = ctx->ensure_io(o_s + sizeof(int) * n + 256);
-  if (st) return st;
-  char* b = ctx->d_io;
-  cudaError_t e = cudaMemcpyAsync(b + o_j, js.jobs.data(), sizeof(CovJob) * n, cudaMemcpyHostToDevice, ctx->stream);
-  if (e != cudaSuccess) return tp_cuda(ctx, e, "cov upload");
   PellProd<R, DIM, KIND> pol;
   memset(&pol, 0, sizeof(pol));
-  pol.jobs = (const CovJob*)(b + o_j);
   pol.hcoef = (sizeof(R) == 8 ? (const R*)(const void*)ctx->d_hcoef : (const R*)(const void*)ctx->d_hcoef32) +
               (size_t)cosmo * HC_COUNT * NNODE;
   CosmoK<R> ck;
-  e = cudaMemcpyAsync(&ck, (const char*)(sizeof(R) == 8 ? ctx->d_ck64 : ctx->d_ck32) + sizeof(CosmoK<R>) * cosmo,
-                      sizeof(ck), cudaMemcpyDeviceToHost, ctx->stream);
+  cudaError_t e = cudaMemcpyAsync(&ck, (const char*)(sizeof(R) == 8 ? ctx->d_ck64 : ctx->d_ck32) + sizeof(CosmoK<R>) * cosmo,
+                                  sizeof(ck), cudaMemcpyDeviceToHost, ctx->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
   if (e != cudaSuccess) return tp_cuda(ctx, e, "cov constants");
   pol.ck = ck;
@@ -536,39 +527,21 @@ static int run_pell_kind(tp_ctx* ctx, int cosmo, const JobSet& js, double theta_
   pol.thetaMax = theta_max;
   pol.thetaMaxY = theta_max_y;
   pol.norm = norm;
-  pol.out = (double*)(b + o_o);
-  pol.status = (int*)(b + o_s);
-  st = run_engine<DIM>(ctx, pol, (int)n, rel_tol);
-  if (st) return st;
-  std::vector<int> hs(n);
-  e = cudaMemcpy(res.data(), b + o_o, sizeof(double) * n, cudaMemcpyDeviceToHost);
-  if (e == cudaSuccess) e = cudaMemcpy(hs.data(), b + o_s, sizeof(int) * n, cudaMemcpyDeviceToHost);
-  if (e != cudaSuccess) return tp_cuda(ctx, e, "cov download");
-  for (size_t i = 0; i < n; ++i) bad += hs[i] != 0;
-  return TP_OK;
+  return run_jobs<DIM>(ctx, pol, js.jobs, rel_tol, 0, res, bad);
 }
 
 template <typename R>
 static int run_t4(tp_ctx* ctx, int cosmo, const JobSet& js, double norm, std::vector<double>& res, int& bad) {
   res.assign(js.jobs.size(), 0.0);
   if (js.jobs.empty()) return TP_OK;
-  const size_t n = js.jobs.size();
-  size_t o_j = 0, o_o = (sizeof(CovJob) * n + 255) & ~size_t(255);
-  size_t o_s = o_o + ((sizeof(double) * n + 255) & ~size_t(255));
-  int st = ctx->ensure_io(o_s + sizeof(int) * n + 256);
-  if (st) return st;
-  char* b = ctx->d_io;
-  cudaError_t e = cudaMemcpyAsync(b + o_j, js.jobs.data(), sizeof(CovJob) * n, cudaMemcpyHostToDevice, ctx->stream);
   BkProd<R> pol;
   memset(&pol, 0, sizeof(pol));
-  pol.jobs = (const CovJob*)(b + o_j);
   pol.ncoef = (sizeof(R) == 8 ? (const R*)(const void*)ctx->d_ncoef64 : (const R*)(const void*)ctx->d_fcoef32) +
               (size_t)cosmo * NCP * NNODE;
   CosmoK<R> ck;
   double ws = 1.0;
-  if (e == cudaSuccess)
-    e = cudaMemcpyAsync(&ck, (const char*)(sizeof(R) == 8 ? ctx->d_ck64 : ctx->d_ck32) + sizeof(CosmoK<R>) * cosmo,
-                        sizeof(ck), cudaMemcpyDeviceToHost, ctx->stream);
+  cudaError_t e = cudaMemcpyAsync(&ck, (const char*)(sizeof(R) == 8 ? ctx->d_ck64 : ctx->d_ck32) + sizeof(CosmoK<R>) * cosmo,
+                                  sizeof(ck), cudaMemcpyDeviceToHost, ctx->stream);
   if (e == cudaSuccess)
     e = cudaMemcpyAsync(&ws, (sizeof(R) == 8 ? ctx->d_wscale64 : ctx->d_wscale32) + cosmo, sizeof(double),
                         cudaMemcpyDeviceToHost, ctx->stream);
@@ -577,16 +550,7 @@ static int run_t4(tp_ctx* ctx, int cosmo, const JobSet& js, double norm, std::ve
   pol.ck = ck;
   pol.wscale = ws;
   pol.norm = norm;
-  pol.out = (double*)(b + o_o);
-  pol.status = (int*)(b + o_s);
-  st = run_engine<5>(ctx, pol, (int)n, 1e-2);
-  if (st) return st;
-  std::vector<int> hs(n);
-  e = cudaMemcpy(res.data(), b + o_o, sizeof(double) * n, cudaMemcpyDeviceToHost);
-  if (e == cudaSuccess) e = cudaMemcpy(hs.data(), b + o_s, sizeof(int) * n, cudaMemcpyDeviceToHost);
-  if (e != cudaSuccess) return tp_cuda(ctx, e, "T4 download");
-  for (size_t i = 0; i < n; ++i) bad += hs[i] != 0;
-  return TP_OK;
+  return run_jobs<5>(ctx, pol, js.jobs, 1e-2, 0, res, bad);
 }
 
 // Evaluates T_term(th6[i]) for all i (single terms, no permutation sums).

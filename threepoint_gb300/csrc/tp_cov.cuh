@@ -7,6 +7,7 @@
 #include <algorithm>
 #include <cstring>
 #include <map>
+#include <string>
 #include <vector>
 
 #include "tp_bispec.cuh"
@@ -102,7 +103,7 @@ __global__ void __launch_bounds__(NT) k_cov(P pol_in, int njobs, int* job_counte
 }
 
 template <int DIM, class P, int CS>
-inline int run_engine_cs(tp_ctx* ctx, const P& pol, int njobs, double rel_tol) {
+inline int run_engine_cs(tp_ctx* ctx, const P& pol, int njobs, double rel_tol, int cap) {
   constexpr int NT = 256;
   if (njobs == 0) return TP_OK;
   auto kern = k_cov<DIM, P, NT, CS>;
@@ -135,10 +136,7 @@ inline int run_engine_cs(tp_ctx* ctx, const P& pol, int njobs, double rel_tol) {
   }
   if (ctx->max_ctas > 0 && units * CS > ctx->max_ctas) units = std::max(1, ctx->max_ctas / CS);
   if (units > njobs) units = njobs;
-  // covariance integrals (6-D square-window T1, oscillating 2-D T2) refine to
-  // 10^5 regions and more: at least 2^19 regions per integral, with the grid
-  // trimmed so that the region stores stay within 64 GB of HBM
-  const int cap = std::max(ctx->region_cap, 1 << 19);
+  // the grid is trimmed so that the region stores stay within 64 GB of HBM
   size_t slot = Slot<DIM, 1>::bytes(cap);
   const size_t budget = size_t(64) << 30;
   if ((size_t)units * slot > budget) units = std::max(1, (int)(budget / slot));
@@ -158,10 +156,15 @@ inline int run_engine_cs(tp_ctx* ctx, const P& pol, int njobs, double rel_tol) {
 // 0 = 8 when the batch has no more integrals than the device has CTA slots
 // (a smaller batch would leave SMs idle, and its most expensive integral
 // would set the time), else 1. A policy whose clusters do not fit runs with 1.
+//
+// cap: regions per integral; 0 = the covariance default (6-D square-window
+// T1, oscillating 2-D T2 and the halo-model terms refine to 10^5 regions and
+// more): at least 2^19.
 template <int DIM, class P>
-inline int run_engine(tp_ctx* ctx, const P& pol, int njobs, double rel_tol, int cluster = 0) {
+inline int run_engine(tp_ctx* ctx, const P& pol, int njobs, double rel_tol, int cluster = 0, int cap = 0) {
   constexpr int NT = 256;
   if (njobs == 0) return TP_OK;
+  if (cap <= 0) cap = std::max(ctx->region_cap, 1 << 19);
   if (cluster == 0) {
     int sms = 0, per_sm = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
@@ -173,11 +176,65 @@ inline int run_engine(tp_ctx* ctx, const P& pol, int njobs, double rel_tol, int 
     cluster = njobs <= sms * per_sm ? 8 : 1;
   }
   if (cluster == 8) {
-    const int st = run_engine_cs<DIM, P, 8>(ctx, pol, njobs, rel_tol);
+    const int st = run_engine_cs<DIM, P, 8>(ctx, pol, njobs, rel_tol, cap);
     if (st != TP_ERR_CUDA || ctx->err.find("cluster occupancy") == std::string::npos) return st;
     cudaGetLastError();  // no 8-CTA cluster of this policy fits: one CTA per integral
   }
-  return run_engine_cs<DIM, P, 1>(ctx, pol, njobs, rel_tol);
+  return run_engine_cs<DIM, P, 1>(ctx, pol, njobs, rel_tol, cap);
+}
+
+// Integrates jobs[i] with policy pol (its jobs / out / status pointers are
+// set here) into res[i]. Integrals that stop at the region cap are integrated
+// again from the start with 16x the cap, up to ctx->escalate_cap regions (the
+// reference's hcubature_v has no cap; the region sequence up to the old cap
+// is the same, so an escalated value is the uncapped one); bad counts the
+// integrals left at a cap or the sweep limit.
+template <int DIM, class P>
+inline int run_jobs(tp_ctx* ctx, P pol, const std::vector<CovJob>& jobs, double rel_tol, int cluster,
+                    std::vector<double>& res, int& bad) {
+  const size_t n = jobs.size();
+  res.assign(n, 0.0);
+  if (n == 0) return TP_OK;
+  std::vector<CovJob> cur = jobs;
+  std::vector<int> where(n);
+  for (size_t i = 0; i < n; ++i) where[i] = (int)i;
+  int cap = std::max(ctx->region_cap, 1 << 19);
+  for (;;) {
+    const size_t m = cur.size();
+    const size_t o_o = (sizeof(CovJob) * m + 255) & ~size_t(255);
+    const size_t o_s = o_o + ((sizeof(double) * m + 255) & ~size_t(255));
+    int st = ctx->ensure_io(o_s + sizeof(int) * m + 256);
+    if (st) return st;
+    char* b = ctx->d_io;
+    cudaError_t e = cudaMemcpyAsync(b, cur.data(), sizeof(CovJob) * m, cudaMemcpyHostToDevice, ctx->stream);
+    if (e != cudaSuccess) return tp_cuda(ctx, e, "cov upload");
+    pol.jobs = (const CovJob*)b;
+    pol.out = (double*)(b + o_o);
+    pol.status = (int*)(b + o_s);
+    st = run_engine<DIM>(ctx, pol, (int)m, rel_tol, cluster, cap);
+    if (st) return st;
+    std::vector<double> v(m);
+    std::vector<int> hs(m);
+    e = cudaMemcpy(v.data(), b + o_o, sizeof(double) * m, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(hs.data(), b + o_s, sizeof(int) * m, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return tp_cuda(ctx, e, "cov download");
+    const int next_cap = (int)std::min<long long>(16LL * cap, ctx->escalate_cap);
+    std::vector<CovJob> again;
+    std::vector<int> again_at;
+    for (size_t i = 0; i < m; ++i) {
+      res[where[i]] = v[i];
+      if ((hs[i] & 1) && next_cap > cap) {
+        again.push_back(cur[i]);
+        again_at.push_back(where[i]);
+      } else if (hs[i]) {
+        ++bad;
+      }
+    }
+    if (again.empty()) return TP_OK;
+    cur.swap(again);
+    where.swap(again_at);
+    cap = next_cap;
+  }
 }
 
 }  // namespace tp

@@ -422,8 +422,11 @@ __device__ void adaptive_body(P& pol, int njobs, int* job_counter, const EngineC
     for (int sweep = 0;; ++sweep) {
       // ---------------- evaluate the pending regions ----------------------
       const int npend = es0->npend;
-      for (int base = crank * CH; base < npend; base += CS * CH) {
-        const int nreg = min(CH, npend - base);
+      // a cluster deals out chunks of CH regions, or single regions while a
+      // sweep has fewer than CS * CH of them (all ranks then have work)
+      const int step = (CS > 1 && npend < CS * CH) ? 1 : CH;
+      for (int base = crank * step; base < npend; base += CS * step) {
+        const int nreg = min(step, npend - base);
         const int npts = nreg * NP;
         // (a) point setup; points that need the expensive inner sums are
         //     appended to a compact live list

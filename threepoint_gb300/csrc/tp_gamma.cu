@@ -334,11 +334,12 @@ struct GammaPolicy {
   }
 };
 
-template <typename R, int NT>
+// CS > 1: one cluster of CS CTAs per integral (cooperative adaptive_body)
+template <typename R, int NT, int CS>
 __global__ void __launch_bounds__(NT, sizeof(R) == 4 ? TP_GAMMA_MINB : 1) k_gamma(GammaPolicy<R> pol_in, int njobs, int* job_counter, EngineCfg cfg,
                                               char* scratch, size_t slot_bytes) {
   GammaPolicy<R> pol = pol_in;
-  adaptive_body<3, 2, NT, GammaPolicy<R>>(pol, njobs, job_counter, cfg, scratch, slot_bytes);
+  adaptive_body<3, 2, NT, GammaPolicy<R>, CS>(pol, njobs, job_counter, cfg, scratch, slot_bytes);
 }
 
 // The Gamma integrand at caller-given points (no cubature): the policy's
@@ -372,23 +373,54 @@ static size_t gamma_smem_bytes() {
 }
 
 constexpr int GAMMA_NT = 256;
+constexpr int GAMMA_CLUSTER = 8;
 
+// max_stores: region stores the launch may use (one per CTA, or per cluster),
+// 0 = no limit beyond ctx->max_ctas. A batch with no more integrals than CTA
+// slots runs one GAMMA_CLUSTER-CTA cluster per integral.
 template <typename R>
 static int run_gamma(tp_ctx* ctx, int cosmo, const double* d_x, const int* d_comp, const int* d_tri, int njobs,
-                     double rel_tol, double* d_out, int* d_status, int cap, int max_ctas) {
+                     double rel_tol, double* d_out, int* d_status, int cap, int max_stores) {
   size_t smem = gamma_smem_bytes<R>();
   cudaError_t e =
-      cudaFuncSetAttribute(k_gamma<R, GAMMA_NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      cudaFuncSetAttribute(k_gamma<R, GAMMA_NT, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return tp_cuda(ctx, e, "gamma attribute");
   int sms = 0, per_sm = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
-  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_gamma<R, GAMMA_NT>, GAMMA_NT, smem);
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_gamma<R, GAMMA_NT, 1>, GAMMA_NT, smem);
   if (e != cudaSuccess || per_sm < 1) return tp_cuda(ctx, e == cudaSuccess ? cudaErrorInvalidConfiguration : e, "gamma occupancy");
-  int grid = sms * per_sm;
-  if (max_ctas > 0 && grid > max_ctas) grid = max_ctas;
-  if (grid > njobs) grid = njobs;
+  int slots = sms * per_sm;
+  if (ctx->max_ctas > 0 && slots > ctx->max_ctas) slots = ctx->max_ctas;
+  int cluster = 1, units = slots;
+  cudaLaunchConfig_t lc = {};
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = GAMMA_CLUSTER;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  lc.blockDim = dim3(GAMMA_NT);
+  lc.dynamicSmemBytes = smem;
+  lc.stream = ctx->stream;
+  lc.attrs = attr;
+  lc.numAttrs = 1;
+  if (njobs <= slots && slots >= GAMMA_CLUSTER) {
+    int ncl = 0;
+    lc.gridDim = dim3(GAMMA_CLUSTER);
+    e = cudaFuncSetAttribute(k_gamma<R, GAMMA_NT, GAMMA_CLUSTER>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)smem);
+    if (e == cudaSuccess)
+      e = cudaOccupancyMaxActiveClusters(&ncl, (const void*)k_gamma<R, GAMMA_NT, GAMMA_CLUSTER>, &lc);
+    cudaGetLastError();
+    ncl = std::min(ncl, slots / GAMMA_CLUSTER);
+    if (e == cudaSuccess && ncl >= 1) {
+      cluster = GAMMA_CLUSTER;
+      units = ncl;
+    }
+  }
+  if (max_stores > 0 && units > max_stores) units = max_stores;
+  if (units > njobs) units = njobs;
   size_t slot = Slot<3, 2>::bytes(cap);
-  int st = ctx->ensure_scratch((size_t)grid * slot);
+  int st = ctx->ensure_scratch((size_t)units * slot);
   if (st) return st;
   GammaPolicy<R> pol;
   pol.J.x = d_x;
@@ -403,8 +435,15 @@ static int run_gamma(tp_ctx* ctx, int cosmo, const double* d_x, const int* d_com
   EngineCfg cfg{0.0, rel_tol, TP_NORM_L1, cap, 2000};
   e = cudaMemsetAsync(ctx->d_counter, 0, sizeof(int), ctx->stream);
   if (e == cudaSuccess) {
-    k_gamma<R, GAMMA_NT><<<grid, GAMMA_NT, smem, ctx->stream>>>(pol, njobs, ctx->d_counter, cfg, ctx->d_scratch, slot);
-    e = cudaGetLastError();
+    if (cluster > 1) {
+      lc.gridDim = dim3(units * GAMMA_CLUSTER);
+      e = cudaLaunchKernelEx(&lc, k_gamma<R, GAMMA_NT, GAMMA_CLUSTER>, pol, njobs, ctx->d_counter, cfg,
+                             ctx->d_scratch, slot);
+    } else {
+      k_gamma<R, GAMMA_NT, 1><<<units, GAMMA_NT, smem, ctx->stream>>>(pol, njobs, ctx->d_counter, cfg, ctx->d_scratch,
+                                                                    slot);
+      e = cudaGetLastError();
+    }
   }
   return tp_cuda(ctx, e, "gamma launch");
 }

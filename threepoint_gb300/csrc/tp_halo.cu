@@ -591,31 +591,13 @@ int run_halo_kind(tp_ctx* ctx, int cosmo, const JobSet& js, double theta_max, do
                   double rel_tol, std::vector<double>& res, int& bad) {
   res.assign(js.jobs.size(), 0.0);
   if (js.jobs.empty()) return TP_OK;
-  const size_t n = js.jobs.size();
-  size_t o_j = 0, o_o = (sizeof(CovJob) * n + 255) & ~size_t(255);
-  size_t o_s = o_o + ((sizeof(double) * n + 255) & ~size_t(255));
-  int st = ctx->ensure_io(o_s + sizeof(int) * n + 256);
-  if (st) return st;
-  char* b = ctx->d_io;
-  cudaError_t e = cudaMemcpyAsync(b + o_j, js.jobs.data(), sizeof(CovJob) * n, cudaMemcpyHostToDevice, ctx->stream);
-  if (e != cudaSuccess) return tp_cuda(ctx, e, "halo term upload");
   HaloProd<KIND, R> pol;
-  st = halo_policy<KIND, R>(ctx, cosmo, theta_max, theta_max_y, norm, pol);
+  int st = halo_policy<KIND, R>(ctx, cosmo, theta_max, theta_max_y, norm, pol);
   if (st) return st;
-  pol.jobs = (const CovJob*)(b + o_j);
-  pol.out = (double*)(b + o_o);
-  pol.status = (int*)(b + o_s);
   // one cluster of 8 CTAs per integral: a T5-T7 point costs 96 nodes x 4-6
   // NFW profiles, so a single integral (or the most expensive one of a batch)
   // spreads over 8 SMs; the region sequence is that of one CTA per integral
-  st = run_engine<HaloProd<KIND, R>::DIM>(ctx, pol, (int)n, rel_tol, ctx->halo_cluster);
-  if (st) return st;
-  std::vector<int> hs(n);
-  e = cudaMemcpy(res.data(), b + o_o, sizeof(double) * n, cudaMemcpyDeviceToHost);
-  if (e == cudaSuccess) e = cudaMemcpy(hs.data(), b + o_s, sizeof(int) * n, cudaMemcpyDeviceToHost);
-  if (e != cudaSuccess) return tp_cuda(ctx, e, "halo term download");
-  for (size_t i = 0; i < n; ++i) bad += hs[i] != 0;
-  return TP_OK;
+  return run_jobs<HaloProd<KIND, R>::DIM>(ctx, pol, js.jobs, rel_tol, ctx->halo_cluster, res, bad);
 }
 
 // the reference's tolerances of the T5, T6, T7 integrals (:1222, :1271, :1307)
@@ -783,6 +765,12 @@ extern "C" int tp_halo_integrand_points(tp_ctx* ctx, int cosmo, int term, int ge
 extern "C" int tp_ctx_set_halo_cluster(tp_ctx* ctx, int ctas) {
   if (!ctx || (ctas != 1 && ctas != 8)) return TP_ERR_ARG;
   ctx->halo_cluster = ctas;
+  return TP_OK;
+}
+
+extern "C" int tp_ctx_set_map3_cluster(tp_ctx* ctx, int on) {
+  if (!ctx || (on != 0 && on != 1)) return TP_ERR_ARG;
+  ctx->map3_cluster = on;
   return TP_OK;
 }
 

@@ -72,6 +72,7 @@ struct Map3Launch {
   const int* job_order;  // optional device permutation of the job indices
   int* job_counter;  // device int
   unsigned* diag;    // device counter of bulk-copy timeouts (may be null)
+  int cluster = 1;   // CTAs per integral (1, or 8 from plan_map3)
 };
 
 // shared memory that the resident CTAs of k_map3<float> hold on one SM
@@ -79,7 +80,11 @@ struct Map3Launch {
 cudaError_t map3_f32_resident_smem(size_t* bytes);
 
 // grid size, dynamic shared memory and scratch bytes of a Map3 launch
-cudaError_t plan_map3(int precision, int njobs, int cap, int max_ctas, int* grid, size_t* smem, size_t* scratch);
+// Launch plan of k_map3: grid, CTAs per integral (1, or 8 when allow_cluster
+// and the batch has no more integrals than CTA slots), dynamic shared memory
+// per CTA and the scratch bytes of the region stores.
+cudaError_t plan_map3(int precision, int njobs, int cap, int max_ctas, int allow_cluster, int* grid, int* cluster,
+                      size_t* smem, size_t* scratch);
 cudaError_t launch_map3(const Map3Launch& L, int grid, size_t smem, char* scratch, cudaStream_t st);
 
 cudaError_t launch_bkappa_points(int precision, const int* cosmo_idx, const double* ell, long n, const void* ncoef,

@@ -12,6 +12,8 @@
 // shared memory with a bulk async copy when the CTA switches cosmology.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include <type_traits>
 
 #include "tp_bispec.cuh"
@@ -262,19 +264,30 @@ struct Map3Policy {
     fv[0] = outer * scale * sum[0];
   }
 
+  // called by rank 0 of a cluster (or the CTA) after the last sweep; the
+  // live-point counters of the other ranks are read through distributed
+  // shared memory (they are reset only at their next job, after a barrier
+  // rank 0 has not yet reached)
   __device__ void end_job(int job, const double* V, const double* E, long long nev, int st) {
     if (threadIdx.x == 0) {
       const double norm = 1. / 8 / PI / PI / PI;
       out[job] = V[0] * norm;
       if (err) err[job] = E[0] * norm;
       if (neval) neval[job] = nev;
-      if (nlive) nlive[job] = (int64_t)*s_live;
+      if (nlive) {
+        unsigned long long live = *s_live;
+        cooperative_groups::cluster_group cl = cooperative_groups::this_cluster();
+        for (unsigned r = 1; r < cl.num_blocks(); ++r) live += *cl.map_shared_rank(s_live, r);
+        nlive[job] = (int64_t)live;
+      }
       if (status) status[job] = st;
     }
   }
 };
 
-template <typename R, int NT>
+// CS > 1: one cluster of CS CTAs per integral (the cooperative form of
+// adaptive_body), for batches with fewer integrals than CTA slots
+template <typename R, int NT, int CS>
 __global__ void __launch_bounds__(NT, sizeof(R) == 4 ? TP_MAP3_MINB : 1) k_map3(Map3Policy<R> pol_in, int njobs, int* job_counter, EngineCfg cfg,
                                              char* scratch, size_t slot_bytes) {
   Map3Policy<R> pol = pol_in;
@@ -283,7 +296,7 @@ __global__ void __launch_bounds__(NT, sizeof(R) == 4 ? TP_MAP3_MINB : 1) k_map3(
   BulkBar* b = pol.bar(smem_);
   if (threadIdx.x == 0) bulkbar_init(b);
   __syncthreads();
-  adaptive_body<3, 1, NT, Map3Policy<R>>(pol, njobs, job_counter, cfg, scratch, slot_bytes);
+  adaptive_body<3, 1, NT, Map3Policy<R>, CS>(pol, njobs, job_counter, cfg, scratch, slot_bytes);
   if (threadIdx.x == 0 && b->timeouts && pol.diag) atomicAdd(pol.diag, b->timeouts);
 }
 
@@ -415,20 +428,62 @@ cudaError_t launch_bkappa_nodes(int precision, int cosmo, const double* ell, lon
 // ---------------------------------------------------------------------------
 constexpr int MAP3_NT = 256;
 
+constexpr int MAP3_CLUSTER = 8;
+
+static cudaLaunchConfig_t map3_launch_config(int grid, size_t smem, cudaStream_t st, int cluster,
+                                             cudaLaunchAttribute* attr) {
+  cudaLaunchConfig_t lc = {};
+  lc.gridDim = dim3(grid);
+  lc.blockDim = dim3(MAP3_NT);
+  lc.dynamicSmemBytes = smem;
+  lc.stream = st;
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = cluster;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  lc.attrs = attr;
+  lc.numAttrs = cluster > 1 ? 1 : 0;
+  return lc;
+}
+
+// grid of CTAs (a multiple of *cluster), one CTA per integral, or, when
+// allow_cluster is set and the batch has no more integrals than CTA slots,
+// one MAP3_CLUSTER-CTA cluster per integral (*cluster = MAP3_CLUSTER);
+// *scratch = bytes of the region stores (one per CTA or per cluster)
 template <typename R>
-static cudaError_t plan_map3_t(int njobs, int cap, int max_ctas, int* grid, size_t* smem, size_t* scratch) {
+static cudaError_t plan_map3_t(int njobs, int cap, int max_ctas, int allow_cluster, int* grid, int* cluster,
+                               size_t* smem, size_t* scratch) {
   *smem = map3_smem_bytes<R>();
+  *cluster = 1;
   cudaError_t e =
-      cudaFuncSetAttribute(k_map3<R, MAP3_NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)*smem);
+      cudaFuncSetAttribute(k_map3<R, MAP3_NT, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)*smem);
   if (e != cudaSuccess) return e;
   int dev = 0, sms = 0, per_sm = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_map3<R, MAP3_NT>, MAP3_NT, *smem);
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_map3<R, MAP3_NT, 1>, MAP3_NT, *smem);
   if (e != cudaSuccess) return e;
   if (per_sm < 1) return cudaErrorInvalidConfiguration;
   int g = sms * per_sm;
   if (max_ctas > 0 && g > max_ctas) g = max_ctas;
+  if (allow_cluster && njobs <= g && (max_ctas <= 0 || max_ctas >= MAP3_CLUSTER)) {
+    int nclusters = 0;
+    cudaLaunchAttribute attr[1];
+    cudaLaunchConfig_t lc = map3_launch_config(MAP3_CLUSTER, *smem, 0, MAP3_CLUSTER, attr);
+    e = cudaFuncSetAttribute(k_map3<R, MAP3_NT, MAP3_CLUSTER>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)*smem);
+    if (e == cudaSuccess)
+      e = cudaOccupancyMaxActiveClusters(&nclusters, (const void*)k_map3<R, MAP3_NT, MAP3_CLUSTER>, &lc);
+    cudaGetLastError();
+    if (e == cudaSuccess && nclusters >= 1) {
+      if (max_ctas > 0) nclusters = std::min(nclusters, max_ctas / MAP3_CLUSTER);
+      nclusters = std::min(nclusters, njobs);
+      *cluster = MAP3_CLUSTER;
+      *grid = nclusters * MAP3_CLUSTER;
+      *scratch = (size_t)nclusters * Slot<3, 1>::bytes(cap);
+      return cudaSuccess;
+    }
+  }
   if (g > njobs) g = njobs;
   if (g < 1) g = 1;
   *grid = g;
@@ -439,19 +494,21 @@ static cudaError_t plan_map3_t(int njobs, int cap, int max_ctas, int* grid, size
 cudaError_t map3_f32_resident_smem(size_t* bytes) {
   const size_t smem = map3_smem_bytes<float>();
   cudaError_t e =
-      cudaFuncSetAttribute(k_map3<float, MAP3_NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      cudaFuncSetAttribute(k_map3<float, MAP3_NT, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   int dev = 0, per_sm = 0, reserved = 0;
   cudaGetDevice(&dev);
-  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_map3<float, MAP3_NT>, MAP3_NT, smem);
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_map3<float, MAP3_NT, 1>, MAP3_NT, smem);
   if (e == cudaSuccess) e = cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, dev);
   *bytes = (size_t)per_sm * (smem + (size_t)reserved);
   return e;
 }
 
-cudaError_t plan_map3(int precision, int njobs, int cap, int max_ctas, int* grid, size_t* smem, size_t* scratch) {
-  return precision == TP_FP64 ? plan_map3_t<double>(njobs, cap, max_ctas, grid, smem, scratch)
-                              : plan_map3_t<float>(njobs, cap, max_ctas, grid, smem, scratch);
+cudaError_t plan_map3(int precision, int njobs, int cap, int max_ctas, int allow_cluster, int* grid, int* cluster,
+                      size_t* smem, size_t* scratch) {
+  return precision == TP_FP64
+             ? plan_map3_t<double>(njobs, cap, max_ctas, allow_cluster, grid, cluster, smem, scratch)
+             : plan_map3_t<float>(njobs, cap, max_ctas, allow_cluster, grid, cluster, smem, scratch);
 }
 
 template <typename R>
@@ -477,7 +534,12 @@ static cudaError_t launch_map3_t(const Map3Launch& L, int grid, size_t smem, cha
   pol.job_order = L.job_order;
   EngineCfg cfg{0.0, L.rel_tol, TP_NORM_L1, L.cap, L.max_sweeps};
   size_t slot = Slot<3, 1>::bytes(L.cap);
-  k_map3<R, MAP3_NT><<<grid, MAP3_NT, smem, st>>>(pol, L.njobs, L.job_counter, cfg, scratch, slot);
+  if (L.cluster == MAP3_CLUSTER) {
+    cudaLaunchAttribute attr[1];
+    cudaLaunchConfig_t lc = map3_launch_config(grid, smem, st, MAP3_CLUSTER, attr);
+    return cudaLaunchKernelEx(&lc, k_map3<R, MAP3_NT, MAP3_CLUSTER>, pol, L.njobs, L.job_counter, cfg, scratch, slot);
+  }
+  k_map3<R, MAP3_NT, 1><<<grid, MAP3_NT, smem, st>>>(pol, L.njobs, L.job_counter, cfg, scratch, slot);
   return cudaGetLastError();
 }
 

@@ -80,9 +80,9 @@ extern "C" int tp_map3_jobs_noalloc(tp_ctx* ctx, const int* job_cosmo_device, co
   if (e != cudaSuccess) return tp_cuda(ctx, e, "set device");
   int st = noalloc_setup(ctx);
   if (st) return st;
-  int grid = 0;
+  int grid = 0, cluster = 1;
   size_t smem = 0, need = 0;
-  e = plan_map3(precision, n_jobs, TP_NOALLOC_REGION_CAP, ctx->max_ctas, &grid, &smem, &need);
+  e = plan_map3(precision, n_jobs, TP_NOALLOC_REGION_CAP, ctx->max_ctas, 0, &grid, &cluster, &smem, &need);
   if (e != cudaSuccess) return tp_cuda(ctx, e, "no-alloc plan");
   // the persistent grid is trimmed to the CTAs whose region stores fit the array
   const size_t slot = need / (size_t)grid;
