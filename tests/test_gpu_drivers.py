@@ -204,3 +204,35 @@ def test_driver_covariance_matrix_layout(nz_file, tmp_path):
     m = np.array([[float(x) for x in r.split()] for r in rows])
     assert np.array_equal(m, m.T)
     assert np.all(np.diag(m) > 0)
+
+
+def test_driver_covariance_halo_terms(nz_file, tmp_path):
+    """T7 and T7_2h through the covariance driver: one radius -> one entry;
+    T7 equals the library's FP32 node sums (the driver's fp32 argument) and
+    T7_2h is the reference's zero."""
+    import threepoint_gb300 as tp
+
+    cos, th, nz = _write_inputs(tmp_path, nz_file)
+    th_file = tmp_path / "thetas1.dat"
+    th_file.write_text("8\n")
+    par = tmp_path / "cov_param.dat"
+    par.write_text("thetaMax 10\nshapenoise_sigma 0.3\ngalaxy_density 36000\nunit deg\nshapenoiseOnly 0\n"
+                   "area 100\n")
+    outdir = tmp_path / "out"
+    outdir.mkdir()
+    _run("calculateApertureStatisticsCovariance", cos, th_file, nz, str(outdir) + "/", par, 0, 0, 0, 0, 0, 1, 1,
+         "infinite", "fp32")
+    cp = tp.covarianceParameters.from_file(str(par))
+    n_deg = cp.galaxy_density / 57.3 / 57.3
+    name = "cov_infinite_term7Numerical_sigma_0.30_n_{:.2f}_thetaMax_{:.2f}_gpu.dat".format(n_deg, cp.theta_max * 57.3)
+    v7 = [float(x) for x in (outdir / name).read_text().split()]
+    v72 = [float(x) for x in (outdir / name.replace("term7Numerical", "term7_2h_Numerical")).read_text().split()]
+    assert v72 == [0.0]
+    ctx = tp.Context(0)
+    ctx.set_shape_noise(cp.shapenoise_sigma, cp.galaxy_density, False)
+    ctx.set_cosmology(tp.cosmology.from_file(cos), tp.read_n_of_z(nz, 256, COSMO1["zmax"]))
+    t = np.array([[8 * ARC] * 3])
+    ref = ctx.cov_total(7, t, t, geometry=tp.GEOM_INFINITE, thetaMax=cp.theta_max, area=cp.area, precision=1)[0]
+    ctx.close()
+    assert len(v7) == 1 and v7[0] != 0
+    assert v7[0] == pytest.approx(ref, rel=1e-5)

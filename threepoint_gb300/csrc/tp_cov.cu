@@ -47,6 +47,7 @@ struct PellProd {
   static constexpr int NL = (KIND <= K_T1_INF) ? 3 : 1;
   static constexpr int G = NL * NCH;
   static constexpr int PD = 1;
+  static constexpr int MINB = 1;
   static constexpr int NS = NL;
   __device__ static int slot(int g) { return g / NCH; }
   static constexpr int CH = (DIM == 6) ? 2 : 8;
@@ -202,6 +203,7 @@ template <typename R>
 struct BkProd {
   static constexpr int G = 16;  // 2 b_kappa x 8 node chunks
   static constexpr int PD = 1;
+  static constexpr int MINB = 1;
   static constexpr int NS = 2;
   __device__ static int slot(int g) { return g >> 3; }
   static constexpr int CH = 4;

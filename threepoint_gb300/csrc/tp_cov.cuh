@@ -94,9 +94,10 @@ struct JobSet {
 // integral (CS = 1) or one cluster of CS CTAs per integral (CS > 1, the
 // cooperative form of adaptive_body, for integrands whose points are costly
 // enough that one integral should spread over several SMs).
+// P::MINB: CTAs per SM the register allocation must allow
 template <int DIM, class P, int NT, int CS>
-__global__ void __launch_bounds__(NT) k_cov(P pol_in, int njobs, int* job_counter, EngineCfg cfg, char* scratch,
-                                            size_t slot_bytes) {
+__global__ void __launch_bounds__(NT, P::MINB) k_cov(P pol_in, int njobs, int* job_counter, EngineCfg cfg,
+                                                     char* scratch, size_t slot_bytes) {
   P pol = pol_in;
   pol.loaded = 0;
   adaptive_body<DIM, 1, NT, P, CS>(pol, njobs, job_counter, cfg, scratch, slot_bytes);

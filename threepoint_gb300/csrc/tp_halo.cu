@@ -40,7 +40,7 @@ __device__ inline double tophat_dw(double x) {
 }
 
 struct SigmaPol {
-  static constexpr int G = 1, PD = 1, NS = 1, CH = 8;
+  static constexpr int G = 1, PD = 1, NS = 1, CH = 8, MINB = 1;
   __device__ static int slot(int) { return 0; }
   struct Rec {
     double v;
@@ -169,6 +169,64 @@ __constant__ SiCiCoef<float> c_sicif = {{TP_SICI_SA}, {TP_SICI_SB}, {TP_SICI_CA}
 
 constexpr double EULER_GAMMA = 0.5772156649;  // the value halomodel.cu:83 uses
 
+// Short FP32 node arithmetic (TP_HALO_FAST_FP32, default on): sin and cos of
+// x >= 0 by reduction to r in [-pi/4, pi/4], x = r + k pi/2 with k = rint(2x/pi)
+// and a three-constant FMA split of pi/2 (Cody & Waite), then the Taylor
+// polynomials of sin (to r^9) and cos (to r^8), whose truncation errors on
+// [-pi/4, pi/4] are below 2e-9 and 3e-8, and the quadrant's swap and signs:
+// absolute error ~1e-7, as the library sincosf of an FP32 argument, in ~20
+// instructions; quotients as reciprocal times numerator (2 ulp); ln on the SFU.
+#ifndef TP_HALO_FAST_FP32
+#define TP_HALO_FAST_FP32 1
+#endif
+#ifndef TP_HALO_F32_CH
+#define TP_HALO_F32_CH 1
+#endif
+#ifndef TP_HALO_F32_MINB
+#define TP_HALO_F32_MINB 3
+#endif
+__device__ __forceinline__ void sincos_r(double x, double* s, double* c) { sincos(x, s, c); }
+__device__ __forceinline__ void sincos_r(float x, float* s, float* c) {
+#if TP_HALO_FAST_FP32
+  const float k = rintf(x * 0.636619772367581343f);  // 2 / pi
+  float r = fmaf(-k, 1.57079637050628662f, x);        // pi/2 rounded to FP32
+  r = fmaf(-k, -4.37113882867379317e-8f, r);          // next FP32 part of pi/2
+  r = fmaf(-k, -1.77635684e-15f, r);                  // remainder
+  const float r2 = r * r;
+  // sin r = r (1 - r^2/3! + r^4/5! - r^6/7! + r^8/9!), cos r = 1 - r^2/2! + ... + r^8/8!
+  float sp = fmaf(r2, 2.75573192e-6f, -1.98412698e-4f);
+  sp = fmaf(sp, r2, 8.33333333e-3f);
+  sp = fmaf(sp, r2, -1.66666667e-1f);
+  const float sr = fmaf(sp * r2, r, r);
+  float cp = fmaf(r2, 2.48015873e-5f, -1.38888889e-3f);
+  cp = fmaf(cp, r2, 4.16666667e-2f);
+  cp = fmaf(cp, r2, -0.5f);
+  const float cr = fmaf(cp, r2, 1.0f);
+  const int q = (int)k & 3;  // x = r + q pi/2 (mod 2 pi)
+  const float sv = (q & 1) ? cr : sr, cv = (q & 1) ? sr : cr;
+  *s = (q & 2) ? -sv : sv;
+  *c = ((q + 1) & 2) ? -cv : cv;
+#else
+  sincosf(x, s, c);
+#endif
+}
+__device__ __forceinline__ double log_r(double x) { return log(x); }
+__device__ __forceinline__ float log_r(float x) {
+#if TP_HALO_FAST_FP32
+  return __logf(x);
+#else
+  return logf(x);
+#endif
+}
+__device__ __forceinline__ double div_r(double a, double b) { return a / b; }
+__device__ __forceinline__ float div_r(float a, float b) {
+#if TP_HALO_FAST_FP32
+  return __fdividef(a, b);
+#else
+  return a / b;
+#endif
+}
+
 template <typename R>
 __device__ __forceinline__ const SiCiCoef<R>& sici_coef() {
   if constexpr (sizeof(R) == 8) return c_sici;
@@ -179,22 +237,19 @@ __device__ __forceinline__ const SiCiCoef<R>& sici_coef() {
 template <typename R>
 __device__ __forceinline__ void sici_small(R x2, R& si_over_x, R& ci_rest_over_x2) {
   const SiCiCoef<R>& k = sici_coef<R>();
-  si_over_x = horner(k.sa, 8, x2) / horner(k.sb, 7, x2);
-  ci_rest_over_x2 = horner(k.ca, 7, x2) / horner(k.cb, 8, x2);
+  si_over_x = div_r(horner(k.sa, 8, x2), horner(k.sb, 7, x2));
+  ci_rest_over_x2 = div_r(horner(k.ca, 7, x2), horner(k.cb, 8, x2));
 }
 // f(x), g(x) for x >= 4
 template <typename R>
 __device__ __forceinline__ void sici_fg(R x, R& f, R& g) {
   const SiCiCoef<R>& k = sici_coef<R>();
-  const R y = (R)1 / (x * x);
-  f = horner(k.fa, 11, y) / (horner(k.fb, 10, y) * x);
-  g = horner(k.ga, 11, y) * y / horner(k.gb, 10, y);
+  const R y = div_r((R)1, x * x);
+  f = div_r(horner(k.fa, 11, y), horner(k.fb, 10, y) * x);
+  g = div_r(horner(k.ga, 11, y) * y, horner(k.gb, 10, y));
 }
 
-__device__ __forceinline__ void sincos_r(double x, double* s, double* c) { sincos(x, s, c); }
-__device__ __forceinline__ void sincos_r(float x, float* s, float* c) { sincosf(x, s, c); }
-__device__ __forceinline__ double log_r(double x) { return log(x); }
-__device__ __forceinline__ float log_r(float x) { return logf(x); }
+
 
 // Truncated NFW profile in Fourier space times F(c) = ln(1+c) - c/(1+c)
 // (u_NFW, halomodel.cu:121-140), with arg1 = k r_200 / c, arg2 = arg1 (1+c):
@@ -233,7 +288,7 @@ __device__ __forceinline__ R u_nfw_f(R a1, R opc, R lnopc) {
     dci = (f2 * s2 - g2 * c2) - (f1 * s1 - g1 * c1);
   }
   const R s12 = s2 * c1 - c2 * s1;  // sin(a2 - a1)
-  return s1 * dsi + c1 * dci - s12 / a2;
+  return s1 * dsi + c1 * dci - div_r(s12, a2);
 }
 
 // ---------------------------------------------------------------------------
@@ -248,7 +303,11 @@ struct HaloProd {
   static constexpr int PD = 1;
   static constexpr int NS = KIND == 5 ? 2 : 1;
   __device__ static int slot(int g) { return KIND == 5 ? (g >= NCH ? 1 : 0) : 0; }
-  static constexpr int CH = 2;
+  // regions per chunk and CTAs per SM: the FP32 form takes one region per
+  // chunk (half the point records and partial sums in shared memory) so that
+  // three CTAs fit on an SM
+  static constexpr int CH = sizeof(R) == 4 ? TP_HALO_F32_CH : 2;
+  static constexpr int MINB = sizeof(R) == 4 ? TP_HALO_F32_MINB : 2;
   struct Rec {
     R l[NL];
     double pm;    // -rhobar/m dsig2/sig2 A (m/rhobar)^n (x the weight scale in FP32): the mass-function factor
@@ -436,7 +495,7 @@ struct HaloProd {
       const R c = r.cm * s_hn[HN_CZ * NNODE + j];
       const R opc = 1 + c;
       const R lnopc = log_r(opc);
-      const R invF = (R)1 / (lnopc - c / opc);
+      const R invF = div_r((R)1, lnopc - div_r(c, opc));
       const R a = r.r200 / c * invchi;
       R prod = fnu * s_hn[(NL == 6 ? HN_WPEN : HN_WTRI) * NNODE + j];
 #pragma unroll
