@@ -213,3 +213,40 @@ def test_cluster_of_eight_equals_one_cta(halo_ctx, prec):
         halo_ctx.set_cov_tolerance(5, 0.0)
     assert np.array_equal(one, eight)
     assert np.all(np.isfinite(one)) and np.all(one != 0)
+
+
+def test_given_pk_leaves_mass_tables_on_eisenstein_hu(nz256):
+    """The reference builds sigma^2(m) with its host linear_pk, which ignores a
+    given P(k) table (its Pk_given global is never set): the mass tables of a
+    cosmology with a table equal those without one."""
+    import threepoint_gb300 as tp
+
+    kmin, kmax = 1e-4, 1e2
+    dk = np.log(kmax / kmin) / 256
+    k = kmin * np.exp(dk * np.arange(256))
+    T = O.Tables(COSMO1, nz256)
+    pk = np.array([T.linear_pk(float(x)) for x in k]) * (1 + 0.1 * np.sin(np.log(k)))
+    with tp.Context(0) as a, tp.Context(0) as b:
+        a.set_cosmology(tp.cosmology(**COSMO1), nz256)
+        b.set_cosmology(tp.cosmology(**COSMO1), nz256, pk=pk, dk=dk, kmin=kmin, kmax=kmax)
+        s_a, d_a = a.halo_tables()
+        s_b, d_b = b.halo_tables()
+    assert np.array_equal(s_a, s_b) and np.array_equal(d_a, d_b)
+
+
+def test_t7_box_corner_cosmology_matches_oracle(nz256):
+    """T7 at a corner of the Latin-hypercube box (Omega_m 0.4, sigma_8 0.9,
+    h 0.8, w -0.8, n_s 1.0) at a loose tolerance: FP64 GPU and oracle refine the
+    same regions."""
+    import threepoint_gb300 as tp
+
+    c = dict(h=0.8, sigma8=0.9, omb=0.048, omc=0.4 - 0.048, ns=1.0, w=-0.8, om=0.4, ow=0.6, zmax=3.0)
+    T = O.Tables(c, nz256)
+    T.set_noise(SIG, NGAL, False)
+    with tp.Context(0) as ctx:
+        ctx.set_shape_noise(SIG, NGAL, False)
+        ctx.set_cosmology(tp.cosmology(**c), nz256)
+        ctx.set_cov_tolerance(7, LOOSE[7])
+        got = ctx.cov_term(7, TH6, geometry=2, thetaMax=TMAX, area=AREA)[0]
+    ref = T.cov_T_halo(7, params(2), TH6, LOOSE[7])[0]
+    assert got == pytest.approx(ref, rel=1e-8)
