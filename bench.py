@@ -158,6 +158,7 @@ def run_ours(args):
     ctxs = [tp.Context(local) for _ in range(nctx)]
     for c in ctxs:
         c.set_limits(args.region_cap)
+        c.set_map3_cluster(args.map3_cluster)
     ctx = ctxs[0]
     streams = [torch.cuda.ExternalStream(c.stream_handle, device=local) for c in ctxs]
     stream = streams[0]
@@ -975,6 +976,8 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--region-cap", type=int, default=32768)
+    ap.add_argument("--map3-cluster", type=int, default=1, choices=[0, 1, 2],
+                    help="8-CTA clusters per integral: 0 never, 1 for batches smaller than the CTA slots, 2 always")
     ap.add_argument("--dump-costs", default="")
     ap.add_argument("--no-order", action="store_true")
     ap.add_argument("--no-fp64-plain", action="store_true", help="skip the plain FP64 comparison run")

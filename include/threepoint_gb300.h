@@ -362,7 +362,8 @@ int tp_ctx_set_halo_cluster(tp_ctx* ctx, int ctas);
 
 /* <Map^3> calls (tp_map3_batch, tp_map3_jobs_device) with no more integrals
  * than the device has CTA slots run one 8-CTA cluster per integral when on
- * (1, default); 0 keeps one CTA per integral. Same results bit for bit. */
+ * (1, default); 2 uses clusters for every batch, 0 one CTA per integral
+ * always. Same results bit for bit. */
 int tp_ctx_set_map3_cluster(tp_ctx* ctx, int on);
 
 /* Halo model of T5-T7 (cuda_version/halomodel.cu), built per cosmology on

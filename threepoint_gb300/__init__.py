@@ -526,8 +526,8 @@ class Context:
 
     def set_map3_cluster(self, on=True):
         """<Map^3> batches with no more integrals than CTA slots: one 8-CTA
-        cluster per integral (on) or one CTA (off)."""
-        _check(self._h, lib().tp_ctx_set_map3_cluster(self._h, int(bool(on))))
+        cluster per integral (on) or one CTA (off); 2: clusters for every batch."""
+        _check(self._h, lib().tp_ctx_set_map3_cluster(self._h, 2 if on == 2 else int(bool(on))))
 
     def set_halo_cluster(self, ctas=8):
         """CTAs per T5/T6/T7 integral: 8 (a thread-block cluster) or 1."""

@@ -828,7 +828,7 @@ extern "C" int tp_ctx_set_halo_cluster(tp_ctx* ctx, int ctas) {
 }
 
 extern "C" int tp_ctx_set_map3_cluster(tp_ctx* ctx, int on) {
-  if (!ctx || (on != 0 && on != 1)) return TP_ERR_ARG;
+  if (!ctx || on < 0 || on > 2) return TP_ERR_ARG;
   ctx->map3_cluster = on;
   return TP_OK;
 }

@@ -446,9 +446,10 @@ static cudaLaunchConfig_t map3_launch_config(int grid, size_t smem, cudaStream_t
   return lc;
 }
 
-// grid of CTAs (a multiple of *cluster), one CTA per integral, or, when
-// allow_cluster is set and the batch has no more integrals than CTA slots,
-// one MAP3_CLUSTER-CTA cluster per integral (*cluster = MAP3_CLUSTER);
+// grid of CTAs (a multiple of *cluster), one CTA per integral, or one
+// MAP3_CLUSTER-CTA cluster per integral (*cluster = MAP3_CLUSTER) when
+// allow_cluster is 1 and the batch has no more integrals than CTA slots, or
+// allow_cluster is 2;
 // *scratch = bytes of the region stores (one per CTA or per cluster)
 template <typename R>
 static cudaError_t plan_map3_t(int njobs, int cap, int max_ctas, int allow_cluster, int* grid, int* cluster,
@@ -466,7 +467,7 @@ static cudaError_t plan_map3_t(int njobs, int cap, int max_ctas, int allow_clust
   if (per_sm < 1) return cudaErrorInvalidConfiguration;
   int g = sms * per_sm;
   if (max_ctas > 0 && g > max_ctas) g = max_ctas;
-  if (allow_cluster && njobs <= g && (max_ctas <= 0 || max_ctas >= MAP3_CLUSTER)) {
+  if ((allow_cluster == 2 || (allow_cluster == 1 && njobs <= g)) && (max_ctas <= 0 || max_ctas >= MAP3_CLUSTER)) {
     int nclusters = 0;
     cudaLaunchAttribute attr[1];
     cudaLaunchConfig_t lc = map3_launch_config(MAP3_CLUSTER, *smem, 0, MAP3_CLUSTER, attr);
