@@ -355,9 +355,11 @@ int tp_cov_term_batch(tp_ctx* ctx, int cosmo_index, int term, int geometry, doub
  * 1271, 1307). */
 int tp_ctx_set_cov_tolerance(tp_ctx* ctx, int term, double rel_tol);
 
-/* CTAs that integrate one T5/T6/T7 integral together: 8 (default; a
- * thread-block cluster of 8 CTAs deals out each sweep's regions) or 1 (one
- * CTA per integral). The results are the same bit for bit. */
+/* CTAs that integrate one T5/T6/T7 integral together: 16 (default: a
+ * thread-block cluster of 16 CTAs, a non-portable cluster size, when the batch
+ * has at most 1/16 as many integrals as the device has CTA slots, else 8), 8
+ * (8-CTA clusters) or 1 (one CTA per integral). A cluster deals out each
+ * sweep's regions to its CTAs; the results are the same bit for bit. */
 int tp_ctx_set_halo_cluster(tp_ctx* ctx, int ctas);
 
 /* <Map^3> calls (tp_map3_batch, tp_map3_jobs_device) with no more integrals

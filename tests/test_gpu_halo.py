@@ -197,9 +197,9 @@ def test_geometry_rules(halo_ctx):
 
 @pytest.mark.parametrize("prec", [0, 1])
 def test_cluster_of_eight_equals_one_cta(halo_ctx, prec):
-    """Eight CTAs of a thread-block cluster sharing each integral refine the
-    same regions as one CTA: identical values, for a batch of distinct
-    integrals (the job loop of the clusters) in both precisions."""
+    """Eight (or sixteen) CTAs of a thread-block cluster sharing each integral
+    refine the same regions as one CTA: identical values, for a batch of
+    distinct integrals (the job loop of the clusters) in both precisions."""
     ths = [TH6, [4 * ARC, 8 * ARC, 8 * ARC, 8 * ARC, 8 * ARC, 16 * ARC],
            [16 * ARC, 16 * ARC, 16 * ARC, 8 * ARC, 16 * ARC, 32 * ARC]]
     halo_ctx.set_cov_tolerance(5, LOOSE[5])
@@ -208,10 +208,12 @@ def test_cluster_of_eight_equals_one_cta(halo_ctx, prec):
         one = halo_ctx.cov_term(5, ths, geometry=2, thetaMax=TMAX, area=AREA, precision=prec)
         halo_ctx.set_halo_cluster(8)
         eight = halo_ctx.cov_term(5, ths, geometry=2, thetaMax=TMAX, area=AREA, precision=prec)
+        halo_ctx.set_halo_cluster(16)
+        sixteen = halo_ctx.cov_term(5, ths, geometry=2, thetaMax=TMAX, area=AREA, precision=prec)
     finally:
-        halo_ctx.set_halo_cluster(8)
+        halo_ctx.set_halo_cluster(16)
         halo_ctx.set_cov_tolerance(5, 0.0)
-    assert np.array_equal(one, eight)
+    assert np.array_equal(one, eight) and np.array_equal(one, sixteen)
     assert np.all(np.isfinite(one)) and np.all(one != 0)
 
 

@@ -529,8 +529,9 @@ class Context:
         cluster per integral (on) or one CTA (off); 2: clusters for every batch."""
         _check(self._h, lib().tp_ctx_set_map3_cluster(self._h, 2 if on == 2 else int(bool(on))))
 
-    def set_halo_cluster(self, ctas=8):
-        """CTAs per T5/T6/T7 integral: 8 (a thread-block cluster) or 1."""
+    def set_halo_cluster(self, ctas=16):
+        """CTAs per T5/T6/T7 integral: 16 (a 16-CTA cluster where the batch
+        leaves room, else 8), 8 (8-CTA clusters) or 1."""
         _check(self._h, lib().tp_ctx_set_halo_cluster(self._h, ctas))
 
     def halo_tables(self, cosmo_index=0):

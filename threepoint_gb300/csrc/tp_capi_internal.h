@@ -53,8 +53,9 @@ struct tp_ctx {
   // halo-model tables (covariance terms T5-T7), built per cosmology on first use
   tp::HaloTab* d_halo = nullptr;
   std::vector<char> halo_ready;
-  // CTAs that share one T5-T7 integral (a thread-block cluster; 1 or 8)
-  int halo_cluster = 8;
+  // CTAs that share one T5-T7 integral (a thread-block cluster): 16 (16 when
+  // the batch leaves room for that many per integral, else 8), 8 or 1
+  int halo_cluster = 16;
   // <Map^3> host calls with no more integrals than CTA slots run one 8-CTA
   // cluster per integral (0: always one CTA per integral)
   int map3_cluster = 1;

@@ -48,6 +48,7 @@ struct PellProd {
   static constexpr int G = NL * NCH;
   static constexpr int PD = 1;
   static constexpr int MINB = 1;
+  static constexpr bool CLUSTER16 = false;
   static constexpr int NS = NL;
   __device__ static int slot(int g) { return g / NCH; }
   static constexpr int CH = (DIM == 6) ? 2 : 8;
@@ -204,6 +205,7 @@ struct BkProd {
   static constexpr int G = 16;  // 2 b_kappa x 8 node chunks
   static constexpr int PD = 1;
   static constexpr int MINB = 1;
+  static constexpr bool CLUSTER16 = false;
   static constexpr int NS = 2;
   __device__ static int slot(int g) { return g >> 3; }
   static constexpr int CH = 4;

@@ -110,6 +110,8 @@ inline int run_engine_cs(tp_ctx* ctx, const P& pol, int njobs, double rel_tol, i
   auto kern = k_cov<DIM, P, NT, CS>;
   size_t smem = engine_smem_bytes<DIM, 1, P>();
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  // clusters of more than 8 CTAs are a non-portable size (allowed on GB300)
+  if (e == cudaSuccess && CS > 8) e = cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
   if (e != cudaSuccess) return tp_cuda(ctx, e, "cov attribute");
   cudaLaunchConfig_t lc = {};
   cudaLaunchAttribute attr[1];
@@ -153,10 +155,27 @@ inline int run_engine_cs(tp_ctx* ctx, const P& pol, int njobs, double rel_tol, i
   return tp_cuda(ctx, e, "cov launch");
 }
 
+// CTA slots of the device for policy P with one CTA per integral
+template <int DIM, class P>
+inline int engine_slots(tp_ctx* ctx) {
+  constexpr int NT = 256;
+  int sms = 0, per_sm = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
+  size_t smem = engine_smem_bytes<DIM, 1, P>();
+  cudaFuncSetAttribute(k_cov<DIM, P, NT, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cov<DIM, P, NT, 1>, NT, smem) != cudaSuccess)
+    per_sm = 1;
+  cudaGetLastError();
+  return sms * std::max(per_sm, 1);
+}
+
 // cluster: 1 = one CTA per integral, 8 = one 8-CTA cluster per integral,
 // 0 = 8 when the batch has no more integrals than the device has CTA slots
 // (a smaller batch would leave SMs idle, and its most expensive integral
-// would set the time), else 1. A policy whose clusters do not fit runs with 1.
+// would set the time), else 1; 16 = one 16-CTA cluster per integral when
+// the batch fills no more than the CTA slots that way (policies with
+// P::CLUSTER16), else as 8. A policy whose clusters do not fit runs with the
+// next smaller form.
 //
 // cap: regions per integral; 0 = the covariance default (6-D square-window
 // T1, oscillating 2-D T2 and the halo-model terms refine to 10^5 regions and
@@ -166,15 +185,16 @@ inline int run_engine(tp_ctx* ctx, const P& pol, int njobs, double rel_tol, int 
   constexpr int NT = 256;
   if (njobs == 0) return TP_OK;
   if (cap <= 0) cap = std::max(ctx->region_cap, 1 << 19);
-  if (cluster == 0) {
-    int sms = 0, per_sm = 0;
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device);
-    size_t smem = engine_smem_bytes<DIM, 1, P>();
-    cudaFuncSetAttribute(k_cov<DIM, P, NT, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cov<DIM, P, NT, 1>, NT, smem) != cudaSuccess)
-      per_sm = 1;
-    cudaGetLastError();
-    cluster = njobs <= sms * per_sm ? 8 : 1;
+  if (cluster == 0) cluster = njobs <= engine_slots<DIM, P>(ctx) ? 8 : 1;
+  if constexpr (P::CLUSTER16) {
+    if (cluster == 16) {
+      if ((long)njobs * 16 <= (long)engine_slots<DIM, P>(ctx)) {
+        const int st = run_engine_cs<DIM, P, 16>(ctx, pol, njobs, rel_tol, cap);
+        if (st != TP_ERR_CUDA || ctx->err.find("cluster") == std::string::npos) return st;
+        cudaGetLastError();  // no 16-CTA cluster fits: 8-CTA clusters
+      }
+      cluster = 8;
+    }
   }
   if (cluster == 8) {
     const int st = run_engine_cs<DIM, P, 8>(ctx, pol, njobs, rel_tol, cap);
@@ -190,16 +210,20 @@ inline int run_engine(tp_ctx* ctx, const P& pol, int njobs, double rel_tol, int 
 // reference's hcubature_v has no cap; the region sequence up to the old cap
 // is the same, so an escalated value is the uncapped one); bad counts the
 // integrals left at a cap or the sweep limit.
+//
+// first_cap: regions of the first pass (0 = the covariance default, at least
+// 2^19). A small first cap sends the few expensive integrals of a batch to
+// the later passes, which hold few integrals and so run on larger clusters.
 template <int DIM, class P>
 inline int run_jobs(tp_ctx* ctx, P pol, const std::vector<CovJob>& jobs, double rel_tol, int cluster,
-                    std::vector<double>& res, int& bad) {
+                    std::vector<double>& res, int& bad, int first_cap = 0) {
   const size_t n = jobs.size();
   res.assign(n, 0.0);
   if (n == 0) return TP_OK;
   std::vector<CovJob> cur = jobs;
   std::vector<int> where(n);
   for (size_t i = 0; i < n; ++i) where[i] = (int)i;
-  int cap = std::max(ctx->region_cap, 1 << 19);
+  int cap = first_cap > 0 ? first_cap : std::max(ctx->region_cap, 1 << 19);
   for (;;) {
     const size_t m = cur.size();
     const size_t o_o = (sizeof(CovJob) * m + 255) & ~size_t(255);

@@ -41,6 +41,7 @@ __device__ inline double tophat_dw(double x) {
 
 struct SigmaPol {
   static constexpr int G = 1, PD = 1, NS = 1, CH = 8, MINB = 1;
+  static constexpr bool CLUSTER16 = false;
   __device__ static int slot(int) { return 0; }
   struct Rec {
     double v;
@@ -308,6 +309,7 @@ struct HaloProd {
   // three CTAs fit on an SM
   static constexpr int CH = sizeof(R) == 4 ? TP_HALO_F32_CH : 2;
   static constexpr int MINB = sizeof(R) == 4 ? TP_HALO_F32_MINB : 2;
+  static constexpr bool CLUSTER16 = true;
   struct Rec {
     R l[NL];
     double pm;    // -rhobar/m dsig2/sig2 A (m/rhobar)^n (x the weight scale in FP32): the mass-function factor
@@ -656,7 +658,14 @@ int run_halo_kind(tp_ctx* ctx, int cosmo, const JobSet& js, double theta_max, do
   // one cluster of 8 CTAs per integral: a T5-T7 point costs 96 nodes x 4-6
   // NFW profiles, so a single integral (or the most expensive one of a batch)
   // spreads over 8 SMs; the region sequence is that of one CTA per integral
-  return run_jobs<HaloProd<KIND, R>::DIM>(ctx, pol, js.jobs, rel_tol, ctx->halo_cluster, res, bad);
+  // A batch too large for 16-CTA clusters runs a first pass that stops at the
+  // context's region cap (32768 by default); the integrals that need more (the
+  // smallest radii) continue in the escalation passes, a handful at a time on
+  // 16-CTA clusters, instead of setting the batch's time on 8 CTAs.
+  constexpr int D = HaloProd<KIND, R>::DIM;
+  const bool big = ctx->halo_cluster == 16 &&
+                   (long)js.jobs.size() * 16 > (long)engine_slots<D, HaloProd<KIND, R>>(ctx);
+  return run_jobs<D>(ctx, pol, js.jobs, rel_tol, ctx->halo_cluster, res, bad, big ? ctx->region_cap : 0);
 }
 
 // the reference's tolerances of the T5, T6, T7 integrals (:1222, :1271, :1307)
@@ -822,7 +831,7 @@ extern "C" int tp_halo_integrand_points(tp_ctx* ctx, int cosmo, int term, int ge
 }
 
 extern "C" int tp_ctx_set_halo_cluster(tp_ctx* ctx, int ctas) {
-  if (!ctx || (ctas != 1 && ctas != 8)) return TP_ERR_ARG;
+  if (!ctx || (ctas != 1 && ctas != 8 && ctas != 16)) return TP_ERR_ARG;
   ctx->halo_cluster = ctas;
   return TP_OK;
 }
