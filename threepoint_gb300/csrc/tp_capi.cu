@@ -586,6 +586,12 @@ extern "C" int tp_ctx_set_escalation(tp_ctx* ctx, int max_region_cap) {
   return TP_OK;
 }
 
+extern "C" int tp_ctx_set_map3_cluster(tp_ctx* ctx, int on) {
+  if (!ctx || on < 0 || on > 2) return TP_ERR_ARG;
+  ctx->map3_cluster = on;
+  return TP_OK;
+}
+
 extern "C" int tp_map3_jobs_device(tp_ctx* ctx, const int* job_cosmo, const double* job_theta, int n_jobs,
                                    double phi_min, double phi_max, double l_min, double l_max, double rel_tol,
                                    int precision, double* out, double* err, int64_t* neval, int64_t* nlive,

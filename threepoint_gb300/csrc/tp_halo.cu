@@ -836,12 +836,6 @@ extern "C" int tp_ctx_set_halo_cluster(tp_ctx* ctx, int ctas) {
   return TP_OK;
 }
 
-extern "C" int tp_ctx_set_map3_cluster(tp_ctx* ctx, int on) {
-  if (!ctx || on < 0 || on > 2) return TP_ERR_ARG;
-  ctx->map3_cluster = on;
-  return TP_OK;
-}
-
 extern "C" int tp_ctx_set_cov_tolerance(tp_ctx* ctx, int term, double rel_tol) {
   if (!ctx || term < 5 || term > 7 || !(rel_tol >= 0)) return TP_ERR_ARG;
   ctx->cov_rel_tol[term] = rel_tol;
