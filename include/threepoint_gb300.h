@@ -350,6 +350,14 @@ int tp_cov_total_batch(tp_ctx* ctx, int cosmo_index, int term, int geometry, dou
 int tp_cov_term_batch(tp_ctx* ctx, int cosmo_index, int term, int geometry, double theta_max, double area,
                       const double* th6, int n, int precision, double* out, int* n_capped);
 
+/* The argument patterns of T_term_total(th123, th456) as this library sums
+ * them (the reference's T1/T2/T4/T5/T6/T7_total branches): for k < return
+ * value, multiplicity mult[k] times T_term of the radii (a0, a1, a2, b0, b1,
+ * b2)[idx[6k + j]], j < 6. Host only; -1 for a bad term or fewer than needed
+ * entries (cap); 0 terms for T2 and T6 of the infinite geometry. */
+int tp_cov_total_terms(int term, int geometry, const double* th123, const double* th456, int* mult, int* idx,
+                       int cap);
+
 /* Relative tolerance of the T5 / T6 / T7 integrals (term 5..7); 0 restores
  * the reference's 1e-2 / 1e-1 / 1e-1 (apertureStatisticsCovariance.cu:1222,
  * 1271, 1307). */

@@ -103,6 +103,8 @@ def lib():
         L.orc_G_square.restype = d
         L.orc_G_square.argtypes = [d, d, d]
         L.orc_halo_tables.argtypes = [p, dp]
+        L.orc_total_probe.restype = d
+        L.orc_total_probe.argtypes = [i, i, p, dp, dp]
         L.orc_halo_ctx_create.restype = p
         L.orc_halo_ctx_create.argtypes = [p, cp, i, dp]
         L.orc_halo_ctx_destroy.argtypes = [p]

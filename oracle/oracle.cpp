@@ -1543,9 +1543,8 @@ double call(TermFn f, const orc_tables* t, const orc_cov_params* p, double a, do
 }  // namespace
 
 // T1_total, apertureStatisticsCovariance.cu:272-326
-extern "C" double orc_T1_total(const orc_tables* t, const orc_cov_params* p, const double* A, const double* B) {
+static double T1_total_with(TermFn f, const orc_tables* t, const orc_cov_params* p, const double* A, const double* B) {
   double t0 = A[0], t1 = A[1], t2 = A[2], t3 = B[0], t4 = B[1], t5 = B[2];
-  TermFn f = t1fn;
   double r;
   if (t3 == t4) {
     if (t4 == t5)
@@ -1568,10 +1567,9 @@ extern "C" double orc_T1_total(const orc_tables* t, const orc_cov_params* p, con
 }
 
 // T2_total, apertureStatisticsCovariance.cu:328-538
-extern "C" double orc_T2_total(const orc_tables* t, const orc_cov_params* p, const double* A, const double* B) {
+static double T2_total_with(TermFn f, const orc_tables* t, const orc_cov_params* p, const double* A, const double* B) {
   if (p->type == 2) return 0;
   double a0 = A[0], a1 = A[1], a2 = A[2], b0 = B[0], b1 = B[1], b2 = B[2];
-  TermFn f = t2fn;
   auto T = [&](double x0, double x1, double x2, double y0, double y1, double y2) { return call(f, t, p, x0, x1, x2, y0, y1, y2); };
   double r;
   // the nine first-triplet cases of the reference, written as (multiplicity, args)
@@ -1611,9 +1609,8 @@ extern "C" double orc_T2_total(const orc_tables* t, const orc_cov_params* p, con
 
 // T4_total, apertureStatisticsCovariance.cu:540-683 (argument patterns kept
 // as the reference evaluates them, including its uneven th4==th5 branch)
-extern "C" double orc_T4_total(const orc_tables* t, const orc_cov_params* p, const double* A, const double* B) {
+static double T4_total_with(TermFn f, const orc_tables* t, const orc_cov_params* p, const double* A, const double* B) {
   double t0 = A[0], t1 = A[1], t2 = A[2], t3 = B[0], t4 = B[1], t5 = B[2];
-  TermFn f = t4fn;
   auto T = [&](double x0, double x1, double x2, double y0, double y1, double y2) { return call(f, t, p, x0, x1, x2, y0, y1, y2); };
   double r;
   if (t0 == t1 && t0 == t2) {
@@ -1633,6 +1630,33 @@ extern "C" double orc_T4_total(const orc_tables* t, const orc_cov_params* p, con
     r = T(t3, t0, t1, t2, t4, t5) + T(t3, t0, t2, t1, t4, t5) + T(t3, t1, t2, t0, t4, t5) + T(t4, t0, t1, t2, t3, t5) + T(t4, t0, t2, t1, t3, t5) + T(t4, t1, t2, t0, t3, t5) + T(t5, t0, t1, t2, t3, t4) + T(t5, t0, t2, t1, t3, t4) + T(t5, t1, t2, t0, t3, t4);
   }
   return r;
+}
+
+extern "C" double orc_T1_total(const orc_tables* t, const orc_cov_params* p, const double* A, const double* B) {
+  return T1_total_with(t1fn, t, p, A, B);
+}
+extern "C" double orc_T2_total(const orc_tables* t, const orc_cov_params* p, const double* A, const double* B) {
+  return T2_total_with(t2fn, t, p, A, B);
+}
+extern "C" double orc_T4_total(const orc_tables* t, const orc_cov_params* p, const double* A, const double* B) {
+  return T4_total_with(t4fn, t, p, A, B);
+}
+
+// The totals of T1, T2, T4 with the term replaced by probe(th6): checks the
+// argument patterns and multiplicities of another implementation of the
+// totals without integrating anything (geometry 1 = square, 2 = infinite).
+namespace {
+double (*g_probe)(const double*) = nullptr;
+double probe_fn(const orc_tables*, const orc_cov_params*, const double* th) { return g_probe(th); }
+}  // namespace
+extern "C" double orc_total_probe(int term, int geometry, double (*probe)(const double*), const double* A,
+                                  const double* B) {
+  g_probe = probe;
+  orc_cov_params p{};
+  p.type = geometry;
+  if (term == 1) return T1_total_with(probe_fn, nullptr, &p, A, B);
+  if (term == 2) return T2_total_with(probe_fn, nullptr, &p, A, B);
+  return T4_total_with(probe_fn, nullptr, &p, A, B);
 }
 
 // ===========================================================================

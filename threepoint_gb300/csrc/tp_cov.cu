@@ -781,6 +781,25 @@ extern "C" int tp_cov_total_batch(tp_ctx* ctx, int cosmo, int term, int geometry
   return TP_OK;
 }
 
+extern "C" int tp_cov_total_terms(int term, int geometry, const double* th123, const double* th456, int* mult,
+                                  int* idx, int cap) {
+  if (!th123 || !th456 || !mult || !idx || cap < 0) return -1;
+  if (term != 1 && term != 2 && (term < 4 || term > 7)) return -1;
+  if ((term == 2 || term == 6) && geometry == TP_GEOM_INFINITE) return 0;
+  const std::vector<PermTerm> t = term == 1   ? t1_terms(th123, th456)
+                                  : term == 2 ? t2_terms(th123, th456)
+                                  : term == 4 ? t4_terms(th123, th456)
+                                  : term == 5 ? t5_terms(th123, th456)
+                                  : term == 6 ? t6_terms(th123, th456)
+                                              : t7_terms(th123, th456);
+  if ((int)t.size() > cap) return -1;
+  for (size_t k = 0; k < t.size(); ++k) {
+    mult[k] = t[k].mult;
+    for (int j = 0; j < 6; ++j) idx[6 * k + j] = t[k].idx[j];
+  }
+  return (int)t.size();
+}
+
 extern "C" int tp_pell_batch(tp_ctx* ctx, int cosmo, const double* ell, long n, int precision, double* out) {
   if (!ctx || !ell || !out || n < 0) return TP_ERR_ARG;
   if (cosmo < 0 || cosmo >= ctx->n_cosmo) return tp_fail(ctx, TP_ERR_STATE, "no such cosmology");
