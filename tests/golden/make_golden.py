@@ -88,9 +88,9 @@ def main():
     T.set_noise(0.3, 10 / O.ARCMIN ** 2, False)
     deg = 0.017453
     g["halo_ref_cubature"] = []
-    for term, geom, rel in ((5, 2, 0.2), (6, 1, 0.5), (7, 2, 0.3)):
+    for term, geom, rel in ((5, 2, 0.2), (6, 1, 0.5), (6, 3, 0.5), (7, 2, 0.3)):
         th6 = [x * O.ARCMIN for x in (8, 8, 16, 8, 16, 16)]
-        par = O.CovParams(geom, 10 * deg, 100 * deg * deg, 0.0)
+        par = O.CovParams(geom, 10 * deg, 100 * deg * deg, 0.0, 5 * deg)
         h = L.orc_halo_ctx_create(T._h, C.byref(par), term, O._dp(np.array(th6)))
         lmax = L.orc_halo_ctx_lmax(h)
         ll, lh = math.log(1e-4), math.log(lmax)
@@ -103,7 +103,8 @@ def main():
         R.ref_hcubature_v(1, C.c_void_p(fp), h, ndim, O._dp(xmin), O._dp(xmax), 0, 0, rel, 3, O._dp(v), O._dp(e))
         L.orc_halo_ctx_destroy(h)
         g["halo_ref_cubature"].append({"term": term, "geometry": geom, "rel": rel, "theta_arcmin": [8, 8, 16, 8, 16, 16],
-                                       "thetaMax_deg": 10, "area_deg2": 100, "sigma": 0.3, "n_arcmin2": 10,
+                                       "thetaMax_deg": 10, "thetaMaxSmaller_deg": 5, "area_deg2": 100,
+                                       "sigma": 0.3, "n_arcmin2": 10,
                                        "raw_value": v[0], "raw_err": e[0]})
     path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "reference_host.json")
     with open(path, "w") as f:

@@ -221,7 +221,8 @@ def test_halo_cubature_bit_identical_to_reference(oracle_tables):
     deg = 0.017453
     for g in GOLD["halo_ref_cubature"]:
         T.set_noise(g["sigma"], g["n_arcmin2"] / O.ARCMIN ** 2, False)
-        par = O.CovParams(g["geometry"], g["thetaMax_deg"] * deg, g["area_deg2"] * deg * deg, 0.0)
+        par = O.CovParams(g["geometry"], g["thetaMax_deg"] * deg, g["area_deg2"] * deg * deg, 0.0,
+                          g.get("thetaMaxSmaller_deg", 0.0) * deg)
         th6 = [x * O.ARCMIN for x in g["theta_arcmin"]]
         h = O.lib().orc_halo_ctx_create(T._h, C.byref(par), g["term"], O._dp(np.array(th6)))
         lmax = O.lib().orc_halo_ctx_lmax(h)
