@@ -2,9 +2,12 @@
 // include/threepoint_gb300_compat.hpp: the calls and globals of
 // calculateApertureStatistics.cu, calculateGamma.cu and
 // calculateApertureStatisticsCovariance.cu, one value each.
-//   compat_example cosmo.param nz.dat
+//   compat_example cosmo.param nz.dat [halo]
 // prints: Map3(8',8',16')  Re Gamma0  Im Gamma0  T2_total(square)
+// [and, with "halo", T7_total(infinite) after initHalomodel, as the
+// covariance driver calls them]
 #include <cstdio>
+#include <string>
 
 #include "threepoint_gb300_compat.hpp"
 
@@ -30,6 +33,13 @@ int main(int argc, char** argv) {
     initCovariance();
     double t2 = T2_total({a, a, b}, {a, b, b});
     printf("%.17g %.17g %.17g %.17g\n", m3, g0.real(), g0.imag(), t2);
+    if (argc > 3 && std::string(argv[3]) == "halo") {
+      constant_powerspectrum = false;
+      type = 2;
+      initCovariance();
+      initHalomodel();
+      printf("%.17g\n", T7_total({a, a, b}, {a, b, b}));
+    }
   } catch (const std::exception& e) {
     fprintf(stderr, "%s\n", e.what());
     return 1;
