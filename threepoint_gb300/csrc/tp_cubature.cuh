@@ -11,8 +11,10 @@
 //
 // GB300 mapping: one CTA owns one integral for its whole adaptive life (a
 // persistent grid pulls integrals from an atomic job counter), so no CTA ever
-// waits on another. Region state lives in a per-CTA slot of HBM scratch
-// (structure of arrays, FP64). Inside a sweep the CTA evaluates the new
+// waits on another; for small batches the CTAs of a thread-block cluster own
+// one integral together (adaptive_body with CS > 1, below), synchronised by
+// the hardware cluster barrier only. Region state lives in a per-CTA (per
+// cluster) slot of HBM scratch (structure of arrays, FP64). Inside a sweep the CTA evaluates the new
 // regions' cubature points in chunks; each point's integrand is split into G
 // independent partial sums (for the line-of-sight integrands: G groups of
 // nodes), giving (point x group) parallelism even for one-region sweeps. The
