@@ -11,7 +11,7 @@
 //   gamma0..gamma3, compute_weights_bessel (gamma.cuh:56-97,291),
 //   the covariance globals type, thetaMax, thetaMax_smaller, area, lMin,
 //   sigma, n, constant_powerspectrum and initCovariance, T1_total, T2_total,
-//   T4_total, T5_total, T6_total, T7_total, initHalomodel
+//   T4_total, T5_total, T6_total, T7_total, T7_2h_total, initHalomodel
 //   (apertureStatisticsCovariance.cuh:22-54,116-136; bispectrum.cuh:19,29;
 //   halomodel.cuh).
 // Differences: errors throw std::runtime_error (or std::invalid_argument)
@@ -207,4 +207,14 @@ inline double T6_total(const std::vector<double>& thetas_123, const std::vector<
 }
 inline double T7_total(const std::vector<double>& thetas_123, const std::vector<double>& thetas_456) {
   return threepoint_gb300_detail::cov_total(7, thetas_123, thetas_456);
+}
+// T7_2h_total (apertureStatisticsCovariance.cu:1046-1063, 1315-1356): 0 for the
+// infinite survey; for the square the reference's integrand multiplies by a
+// survey-variance table it never fills (dev_sigma2_from_windowfunction_array),
+// so its value is 0 as well; the other geometries throw, as the reference does.
+inline double T7_2h_total(const std::vector<double>& thetas_123, const std::vector<double>& thetas_456) {
+  if (thetas_123.size() != 3 || thetas_456.size() != 3)
+    throw std::invalid_argument("T7_2h_total: Wrong number of aperture radii");
+  if (type == 2 || type == 1) return 0.0;
+  throw std::logic_error("T7_SSC: Wrong survey geometry, only coded for square survey");
 }

@@ -38,7 +38,7 @@ int main(int argc, char** argv) {
       type = 2;
       initCovariance();
       initHalomodel();
-      printf("%.17g\n", T7_total({a, a, b}, {a, b, b}));
+      printf("%.17g %.17g\n", T7_total({a, a, b}, {a, b, b}), T7_2h_total({a, a, b}, {a, b, b}));
     }
   } catch (const std::exception& e) {
     fprintf(stderr, "%s\n", e.what());

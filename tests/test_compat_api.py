@@ -56,3 +56,17 @@ def test_compat_values_match_python_api(tmp_path, nz_file, nz256):
     ref = ctx.T2_total([a, a, b], [a, b, b], geometry=tp.GEOM_SQUARE, thetaMax=tmax, area=tmax * tmax)
     assert t2 == pytest.approx(ref, rel=1e-12)
     ctx.close()
+
+
+def test_t7_2h_total_is_the_references_zero():
+    """T7_2h of the reference is 0 for the square and infinite surveys (its
+    integrand's variance table is never filled) and throws for the others."""
+    import threepoint_gb300 as tp
+
+    a, b = [1e-3] * 3, [2e-3] * 3
+    assert tp.Context.T7_2h_total(a, b, geometry=tp.GEOM_SQUARE) == 0.0
+    assert tp.Context.T7_2h_total(a, b, geometry=tp.GEOM_INFINITE) == 0.0
+    for g in (tp.GEOM_CIRCLE, tp.GEOM_RECTANGLE):
+        with pytest.raises(ValueError):
+            tp.Context.T7_2h_total(a, b, geometry=g)
+

@@ -518,6 +518,18 @@ class Context:
     def T7_total(self, th123, th456, **kw):
         return float(self.cov_total(7, [th123], [th456], **kw)[0])
 
+    @staticmethod
+    def T7_2h_total(th123, th456, geometry=GEOM_SQUARE, **kw):
+        """T7_2h_total (apertureStatisticsCovariance.cu:1046-1063,1315-1356):
+        0 for the infinite survey, and 0 for the square because the reference's
+        integrand multiplies by a survey-variance table it never fills; the
+        reference throws for the circle and the rectangle (ValueError here)."""
+        if len(th123) != 3 or len(th456) != 3:
+            raise ValueError("T7_2h_total: Wrong number of aperture radii")
+        if geometry in (GEOM_SQUARE, GEOM_INFINITE):
+            return 0.0
+        raise ValueError("T7_SSC: Wrong survey geometry, only coded for square survey")
+
     # -- halo model (cuda_version/halomodel.cu) --
     def set_cov_tolerance(self, term, rel_tol):
         """Relative tolerance of the T5/T6/T7 integrals (0 = the reference's
